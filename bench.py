@@ -1,0 +1,534 @@
+#!/usr/bin/env python3
+"""Benchmark of the GQF bulk hot path at 2^28 slots and 90% load.
+
+Workload (one "step", the reference's large bulk configuration): an empty
+2^28-slot filter is filled to 90% load with 241,591,910 uniform uint64 keys
+(splitmix64, seed 1) in bulk_insert batches of 2^24 keys; then bulk_get of
+2^26 present keys and 2^26 absent keys (splitmix64, seed 2); then bulk_delete
+of the 2^26 present keys.  Metric: key operations per second over the whole
+step (inserts + gets + deletes), in Mkeys/s; per-operation rates are reported
+beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default) prints one JSON line with the device-resident value,
+the end-to-end value through the C ABI from pinned host buffers (copies in
+the timed region), the roofline of the dominant kernel, a CPU baseline, SM
+clocks sampled during the timed region and the number of library kernel
+launches.  --impl reference times the reference's CPU implementation of the
+same path (the oracle restatement, multi-threaded over regions the way the
+reference's launch is) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bulk insert/get Mkeys/s at 2^28 slots 90% load vs ref CUDA; serving p99 ms"
+UNIT = "Mkeys/s"
+# algorithmic bytes per key (reference packed format)
+BYTES_GET = 97.0          # 8 key in + 8 count out + one 81-byte block
+BLOCK_BYTES = 81.0
+PART_BYTES_PER_KEY = 16.0  # key read + partitioned key written
+REBUILD_KEY_BYTES = 8.0    # partitioned key read back
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nbits", type=int, default=28)
+    ap.add_argument("--batch-log", type=int, default=24)
+    ap.add_argument("--get-log", type=int, default=26)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    return ap.parse_args()
+
+
+class Workload:
+    def __init__(self, nbits, batch_log, get_log):
+        self.nbits = nbits
+        self.nslots = 1 << nbits
+        self.n_insert = int(0.9 * self.nslots)
+        self.batch = 1 << batch_log
+        self.n_get = min(1 << get_log, self.n_insert)
+        self.batches = [(i, min(self.batch, self.n_insert - i)) for i in range(0, self.n_insert, self.batch)]
+        self.xnslots = self.nslots + int(10 * np.sqrt(self.nslots))
+        self.nblocks = (self.xnslots + 63) // 64
+
+    @property
+    def key_ops(self):
+        return self.n_insert + 2 * self.n_get + self.n_get
+
+    def touched_blocks(self, b):
+        return self.nblocks * (1.0 - np.exp(-b / self.nblocks))
+
+    def describe(self):
+        return {
+            "workload": f"config 2: nbits={self.nbits} ({self.nslots} slots), fill 90% ({self.n_insert} keys) "
+                        f"in {len(self.batches)} bulk_insert batches of 2^{int(np.log2(self.batch))}, "
+                        f"bulk_get {self.n_get} present + {self.n_get} absent, bulk_delete {self.n_get} present",
+            "nbits": self.nbits,
+            "keys_inserted": self.n_insert,
+            "insert_batch": self.batch,
+            "gets_present": self.n_get,
+            "gets_absent": self.n_get,
+            "deletes": self.n_get,
+            "key_ops_per_step": self.key_ops,
+            "keys": "splitmix64 seed 1 (present), seed 2 (absent)",
+            "l2": "inputs (1.9 GB of keys, 0.4 GB filter) exceed the 129 MB L2; no extra flush",
+        }
+
+
+def splitmix_dev(seed, n, torch):
+    """splitmix64 stream on the device (torch int64 arithmetic wraps)."""
+    out = torch.empty(n, dtype=torch.int64, device="cuda")
+    chunk = 1 << 26
+    g = np.int64(np.uint64(0x9E3779B97F4A7C15).view(np.int64))
+    m1 = np.int64(np.uint64(0xBF58476D1CE4E5B9).view(np.int64))
+    m2 = np.int64(np.uint64(0x94D049BB133111EB).view(np.int64))
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        x = torch.arange(s + 1, e + 1, dtype=torch.int64, device="cuda") * g + seed
+        x = (x ^ ((x >> 30) & ((1 << 34) - 1))) * m1
+        x = (x ^ ((x >> 27) & ((1 << 37) - 1))) * m2
+        out[s:e] = x ^ ((x >> 31) & ((1 << 33) - 1))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+            "power_w_max": max(power) if power else None,
+        }
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the rebuild and probe kernels from the
+    committed ncu summary (profiles/ncu_traffic.json), if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+# --------------------------------------------------------------- GPU arm
+
+def run_gpu(args, wl, rank, world):
+    import torch
+
+    import cqf_gb300
+    from cqf_gb300 import build
+
+    build.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    keys = splitmix_dev(1, wl.n_insert, torch)
+    absent = splitmix_dev(2, wl.n_get, torch)
+    present = keys[: wl.n_get]
+    out = torch.empty(wl.n_get, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+
+    qf = cqf_gb300.QF(wl.nbits)
+
+    def step():
+        qf.reset()
+        for s, n in wl.batches:
+            qf.bulk_insert(keys[s:s + n], n=n)
+        e_ins.record()
+        qf.bulk_get(present, out)
+        qf.bulk_get(absent, out)
+        e_get.record()
+        for s in range(0, wl.n_get, wl.batch):
+            n = min(wl.batch, wl.n_get - s)
+            qf.bulk_delete(present[s:s + n], n=n)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_ins, e_get = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # correctness of the last warm-up step, outside the timed region
+    qf.reset()
+    for s, n in wl.batches:
+        qf.bulk_insert(keys[s:s + n], n=n)
+    qf.bulk_get(present, out)
+    ok_present = bool((out > 0).all().item())
+    qf.bulk_get(absent, out)
+    fp = int((out > 0).sum().item())
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.4)
+    qf.profile(True)
+    launches0 = cqf_gb300.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    per = {"insert": 0.0, "get": 0.0, "delete": 0.0}
+    e0.record()
+    for _ in range(args.steps):
+        s0 = torch.cuda.Event(enable_timing=True)
+        s0.record()
+        step()
+        s1 = torch.cuda.Event(enable_timing=True)
+        s1.record()
+        torch.cuda.synchronize()
+        per["insert"] += s0.elapsed_time(e_ins)
+        per["get"] += e_ins.elapsed_time(e_get)
+        per["delete"] += e_get.elapsed_time(s1)
+    e1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = cqf_gb300.launch_count() - launches0
+    prof = qf.profile_read()
+    qf.profile(False)
+    clk = clocks.stop()
+    status = qf.status()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    value = wl.key_ops * world / (ms * 1e-3) / 1e6
+    ops = {k: {"ms": v / args.steps} for k, v in per.items()}
+    ops["insert"]["mkeys_s"] = wl.n_insert / (ops["insert"]["ms"] * 1e3)
+    ops["get"]["mkeys_s"] = 2 * wl.n_get / (ops["get"]["ms"] * 1e3)
+    ops["delete"]["mkeys_s"] = wl.n_get / (ops["delete"]["ms"] * 1e3)
+
+    # roofline per kernel phase, algorithmic bytes per launch / event time
+    peak, peak_kind = measured_peak()
+    t_ins_blocks = sum(wl.touched_blocks(n) for _, n in wl.batches)
+    t_del_blocks = sum(wl.touched_blocks(min(wl.batch, wl.n_get - s)) for s in range(0, wl.n_get, wl.batch))
+    phases = {
+        "rebuild_insert": (prof["insert"], 2 * BLOCK_BYTES * t_ins_blocks + REBUILD_KEY_BYTES * wl.n_insert),
+        "rebuild_delete": (prof["delete"], 2 * BLOCK_BYTES * t_del_blocks + REBUILD_KEY_BYTES * wl.n_get),
+        "probe_get": (prof["get"], BYTES_GET * 2 * wl.n_get),
+        "partition": (prof["partition"], PART_BYTES_PER_KEY * (wl.n_insert + wl.n_get)),
+    }
+    kernels = {}
+    for name, (p, bytes_per_step) in phases.items():
+        if p["calls"] == 0 or p["ms"] <= 0:
+            continue
+        t_step = p["ms"] / args.steps
+        kernels[name] = {
+            "ms_per_step": t_step,
+            "calls_per_step": p["calls"] // args.steps,
+            "algorithmic_gb_per_step": bytes_per_step / 1e9,
+            "achieved_gbs": bytes_per_step / (t_step * 1e-3) / 1e9,
+        }
+    dom = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
+    d = kernels[dom]
+    traffic = profile_traffic().get(dom)
+    roofline = {
+        "bound": "hbm",
+        "kernel": dom,
+        "achieved": round(d["achieved_gbs"], 1),
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": round(d["achieved_gbs"] / peak, 4),
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "traffic": traffic.get("bytes_per_launch") if traffic else None,
+        "algorithmic_bytes_per_launch": d["algorithmic_gb_per_step"] * 1e9 / max(1, d["calls_per_step"]),
+    }
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, wl, qf, keys, absent, torch)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = run_cpu_sample(wl, keys, absent, args)
+
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic (splitmix64 keys, generated on the device before timing)",
+        "config": wl.describe() | {"parallelism": "replicas" if world > 1 else "single GPU"},
+        "impl": "ours",
+        "ops": {k: {kk: round(vv, 3) for kk, vv in v.items()} for k, v in ops.items()},
+        "kernels": {k: {kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}
+                    for k, v in kernels.items()},
+        "roofline": roofline,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": int(launches // args.steps),
+        "check": {"present_all_found": ok_present, "false_positives_absent": fp, "status": status},
+    }
+    qf.close()
+    if dist:
+        dist.destroy_process_group()
+    return line
+
+
+def run_e2e(args, wl, qf, keys_dev, absent_dev, torch):
+    """The same step through the C ABI from pinned host buffers: every batch
+    is copied host->device inside the timed region, get results come back
+    device->host.  Copies overlap compute on a second stream."""
+    hk = torch.empty(wl.n_insert, dtype=torch.int64, pin_memory=True)
+    ha = torch.empty(wl.n_get, dtype=torch.int64, pin_memory=True)
+    hk.copy_(keys_dev.cpu())
+    ha.copy_(absent_dev.cpu())
+    hres = torch.empty(2 * wl.n_get, dtype=torch.int64, pin_memory=True)
+    comp = torch.cuda.Stream()
+    copy = torch.cuda.Stream()
+    B = wl.batch
+    bufs = [torch.empty(B, dtype=torch.int64, device="cuda") for _ in range(2)]
+    outs = [torch.empty(B, dtype=torch.int64, device="cuda") for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
+    done = [torch.cuda.Event() for _ in range(2)]
+    for e in done:
+        e.record(comp)
+    qf.set_stream(comp)
+
+    def phase(chunks, op):
+        for i, (src, s, n) in enumerate(chunks):
+            b = i & 1
+            copy.wait_event(done[b])
+            with torch.cuda.stream(copy):
+                bufs[b][:n].copy_(src[s:s + n], non_blocking=True)
+                copied[b].record(copy)
+            comp.wait_event(copied[b])
+            if op == "insert":
+                qf.bulk_insert_async(bufs[b], n, stream=comp)
+            elif op == "delete":
+                qf.bulk_delete_async(bufs[b], n, stream=comp)
+            else:
+                qf.bulk_get_async(bufs[b], outs[b], n, stream=comp)
+                with torch.cuda.stream(comp):
+                    off = s + (wl.n_get if src is ha else 0)
+                    hres[off:off + n].copy_(outs[b][:n], non_blocking=True)
+            done[b].record(comp)
+
+    ins = [(hk, s, n) for s, n in wl.batches]
+    gets = [(hk, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)] + \
+           [(ha, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)]
+    dels = [(hk, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)]
+
+    def step():
+        with torch.cuda.stream(comp):
+            qf.reset()
+        phase(ins, "insert")
+        phase(gets, "get")
+        phase(dels, "delete")
+
+    for _ in range(max(1, args.warmup - 1)):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    qf.set_stream(None)
+    found = bool((hres[: wl.n_get] > 0).all().item())
+    h2d = 8 * (wl.n_insert + 2 * wl.n_get + wl.n_get)
+    return {
+        "value": round(wl.key_ops / dt / 1e6, 2),
+        "unit": UNIT,
+        "ms_per_step": round(dt * 1e3, 3),
+        "h2d_bytes_per_step": h2d,
+        "d2h_bytes_per_step": 8 * 2 * wl.n_get,
+        "path": "C ABI (gqf_bulk_*_async) from pinned host buffers, copies on a second stream",
+        "present_all_found": found,
+    }
+
+
+# --------------------------------------------------------------- CPU arms
+
+def cpu_threads(args):
+    return args.cpu_threads or os.cpu_count() or 1
+
+
+def run_cpu_sample(wl, keys_dev, absent_dev, args):
+    """The oracle (the reference's algorithm restated in C) on the host cores,
+    on the full step's inputs once: a bounded sample of about 5-30 s."""
+    import oracle
+
+    oracle.build()
+    keys = keys_dev.cpu().numpy().view(np.uint64)
+    absent = absent_dev.cpu().numpy().view(np.uint64)
+    return cpu_step(wl, keys, absent, cpu_threads(args), oracle, kind="port")
+
+
+def cpu_step(wl, keys, absent, threads, oracle, kind):
+    o = oracle.Oracle(wl.nbits, threads=threads)
+    t0 = time.perf_counter()
+    for s, n in wl.batches:
+        o.bulk_insert(keys[s:s + n])
+    t1 = time.perf_counter()
+    c1 = o.bulk_get(keys[: wl.n_get])
+    c2 = o.bulk_get(absent)
+    t2 = time.perf_counter()
+    for s in range(0, wl.n_get, wl.batch):
+        o.bulk_delete(keys[s:min(wl.n_get, s + wl.batch)])
+    t3 = time.perf_counter()
+    o.close()
+    dt = t3 - t0
+    assert (c1 > 0).all()
+    return {
+        "value": round(wl.key_ops / dt / 1e6, 3),
+        "unit": UNIT,
+        "cores": threads,
+        "kind": kind,
+        "sample": f"the full step once ({wl.key_ops} key ops), {threads} threads: regions of one parity "
+                  f"in parallel, as the reference's even/odd launch; hash + sort single-threaded",
+        "seconds": round(dt, 3),
+        "ops": {"insert_mkeys_s": round(wl.n_insert / (t1 - t0) / 1e6, 3),
+                "get_mkeys_s": round(2 * wl.n_get / (t2 - t1) / 1e6, 3),
+                "delete_mkeys_s": round(wl.n_get / (t3 - t2) / 1e6, 3)},
+    }
+
+
+def run_reference(args, wl, rank, world):
+    """--impl reference: the reference's CPU implementation of the path (the
+    oracle port on this host; the reference's own host code is x86-only) on
+    all host cores, each step one full step of the workload."""
+    if rank != 0:
+        return None
+    import oracle
+
+    oracle.build()
+    keys = oracle.splitmix64(1, wl.n_insert)
+    absent = oracle.splitmix64(2, wl.n_get)
+    threads = cpu_threads(args)
+    for _ in range(args.warmup):
+        cpu_step(wl, keys, absent, threads, oracle, "port")
+    vals, secs = [], []
+    for _ in range(args.steps):
+        r = cpu_step(wl, keys, absent, threads, oracle, "port")
+        vals.append(r["value"])
+        secs.append(r["seconds"])
+    dt = sum(secs) / len(secs)
+    v = wl.key_ops / dt / 1e6
+    return {
+        "metric": METRIC,
+        "value": round(v, 3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic (splitmix64 keys)",
+        "config": wl.describe(),
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step is the full workload ({wl.key_ops} key ops) on {threads} threads"},
+        "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    wl = Workload(args.nbits, args.batch_log, args.get_log)
+    if args.impl == "reference":
+        line = run_reference(args, wl, rank, world)
+    else:
+        line = run_gpu(args, wl, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,286 @@
+"""GB300-native counting quotient filter: Python view of the C ABI.
+
+The product is ``cqf_gb300/_lib/libgqf_gb300.so`` (C ABI in ``include/gqf.h``)
+and ``libgqf_gb300_device.a`` (device point API, ``include/gqf.cuh``), both
+built by :func:`cqf_gb300.build.build`.  This module binds the C ABI with
+ctypes and mirrors the reference's host API (PASSIONLab/cqf include/gqf.cuh)
+for tests and benchmarks: same function names, same argument meaning, same
+asynchronous behaviour.  Device buffers are passed as raw pointers; the
+helpers accept torch CUDA tensors for convenience (torch is only plumbing
+here: device memory and streams).
+
+There is no CPU fallback.  If the native library is missing or cannot be
+loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+QF_NO_LOCK = 0x01
+QF_TRY_ONCE_LOCK = 0x02
+QF_WAIT_FOR_LOCK = 0x04
+QF_KEY_IS_HASH = 0x08
+
+QF_ITEM_INSERTED, QF_ITEM_FOUND, QF_FULL, QF_TIMEOUT = 0, 1, 2, 3
+
+STATUS_FULL = 1 << 0
+STATUS_TIMEOUT = 1 << 1
+STATUS_BAD_KEY = 1 << 2
+STATUS_DEFERRED = 1 << 3
+STATUS_OVERFLOW = 1 << 4
+
+LIB_PATH = _build.SO_PATH
+
+_vp, _u64, _u32, _int, _u8 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint8
+
+# name -> (restype, argtypes); mirrors include/gqf.h
+SIGNATURES = {
+    "qf_malloc_device": (None, [ctypes.POINTER(_vp), _int, ctypes.c_bool]),
+    "qf_destroy_device": (None, [_vp]),
+    "bulk_insert": (None, [_vp, _u64, _vp, _u8]),
+    "bulk_insert_reduce": (None, [_vp, _u64, _vp, _u8]),
+    "bulk_delete": (None, [_vp, _u64, _vp, _u8]),
+    "bulk_get": (None, [_vp, _u64, _vp, _vp]),
+    "bulk_get_misses_wrapper": (_u64, [_vp, _vp, _u64]),
+    "point_get_wrapper": (_u64, [_vp, _vp, _u64]),
+    "gqf_point_bulk_insert": (_int, [_vp, _vp, _u64]),
+    "gqf_point_insert_batch": (_int, [_vp, _vp, _u64, _u8, _vp]),
+    "gqf_point_insert_not_exists_batch": (_int, [_vp, _vp, _u64, _u8, _vp, _vp]),
+    "gqf_point_query_batch": (_int, [_vp, _vp, _u64, _u8, _int, _vp]),
+    "gqf_bulk_insert_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
+    "gqf_bulk_insert_reduce_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
+    "gqf_bulk_delete_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
+    "gqf_bulk_get_async": (_int, [_vp, _u64, _vp, _vp, _u8, _vp]),
+    "gqf_set_stream": (_int, [_vp, _vp]),
+    "gqf_set_region_log": (_int, [_vp, _int]),
+    "gqf_get_region_log": (_int, [_vp]),
+    "gqf_nslots": (_u64, [_vp]),
+    "gqf_xnslots": (_u64, [_vp]),
+    "gqf_nblocks": (_u64, [_vp]),
+    "gqf_device_bytes": (_u64, [_vp]),
+    "gqf_get_status": (_int, [_vp, ctypes.POINTER(_u32)]),
+    "gqf_clear_status": (_int, [_vp]),
+    "gqf_reset": (_int, [_vp]),
+    "gqf_export_size": (_u64, [_vp]),
+    "gqf_export": (_int, [_vp, _vp, _u64]),
+    "gqf_import": (_int, [_vp, _vp, _u64]),
+    "gqf_debug_serial_apply": (_int, [_vp, _vp, _u64, _int]),
+    "gqf_profile": (_int, [_vp, _int]),
+    "gqf_profile_read": (_int, [_vp, _vp, _vp, _vp]),
+    "gqf_launch_count": (_u64, []),
+    "gqf_last_error": (ctypes.c_char_p, []),
+    "gqf_version": (ctypes.c_char_p, []),
+}
+
+_LIB = None
+
+
+def load(path: str | None = None, build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load the native library (raising if it is absent)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"cqf_gb300 native library not built: {p} (run cqf_gb300.build.build())")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().gqf_last_error().decode()
+
+
+def _ptr(x) -> int:
+    """Device pointer of a torch tensor, an int, or None."""
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"expected a device tensor or pointer, got {type(x)}")
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        return 0
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+class QF:
+    """One filter on the current GPU (the reference's QF* handle)."""
+
+    def __init__(self, nbits: int, bulk_config: bool = True, log_region: int | None = None):
+        self.L = load()
+        h = _vp()
+        self.L.qf_malloc_device(ctypes.byref(h), int(nbits), bool(bulk_config))
+        if not h.value:
+            raise RuntimeError("qf_malloc_device failed: " + last_error())
+        self.h = h.value
+        self.nbits = nbits
+        if log_region is not None:
+            self.set_region_log(log_region)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.qf_destroy_device(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- geometry
+    @property
+    def nslots(self) -> int:
+        return int(self.L.gqf_nslots(self.h))
+
+    @property
+    def xnslots(self) -> int:
+        return int(self.L.gqf_xnslots(self.h))
+
+    @property
+    def nblocks(self) -> int:
+        return int(self.L.gqf_nblocks(self.h))
+
+    def set_region_log(self, lr: int):
+        if self.L.gqf_set_region_log(self.h, int(lr)) != 0:
+            raise ValueError(last_error())
+
+    def region_log(self) -> int:
+        return int(self.L.gqf_get_region_log(self.h))
+
+    # ---- reference bulk API (device buffers)
+    def bulk_insert(self, keys, n: int | None = None, flags: int = QF_NO_LOCK):
+        n = keys.numel() if n is None else n
+        self.L.bulk_insert(self.h, n, _ptr(keys), flags)
+
+    def bulk_insert_reduce(self, keys, n: int | None = None, flags: int = QF_NO_LOCK):
+        n = keys.numel() if n is None else n
+        self.L.bulk_insert_reduce(self.h, n, _ptr(keys), flags)
+
+    def bulk_delete(self, keys, n: int | None = None, flags: int = QF_NO_LOCK):
+        n = keys.numel() if n is None else n
+        self.L.bulk_delete(self.h, n, _ptr(keys), flags)
+
+    def bulk_get(self, vals, returns, n: int | None = None):
+        n = vals.numel() if n is None else n
+        self.L.bulk_get(self.h, n, _ptr(vals), _ptr(returns))
+
+    def bulk_get_misses(self, vals, n: int | None = None) -> int:
+        n = vals.numel() if n is None else n
+        return int(self.L.bulk_get_misses_wrapper(self.h, _ptr(vals), n))
+
+    def point_get_misses(self, keys, n: int | None = None) -> int:
+        n = keys.numel() if n is None else n
+        return int(self.L.point_get_wrapper(self.h, _ptr(keys), n))
+
+    # ---- extensions
+    def bulk_insert_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
+        self._ok(self.L.gqf_bulk_insert_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
+
+    def bulk_delete_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
+        self._ok(self.L.gqf_bulk_delete_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
+
+    def bulk_get_async(self, vals, returns, n, flags=0, stream=None):
+        self._ok(self.L.gqf_bulk_get_async(self.h, n, _ptr(vals), _ptr(returns), flags, _stream_ptr(stream)))
+
+    def point_bulk_insert(self, keys, n=None):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_point_bulk_insert(self.h, _ptr(keys), n))
+
+    def point_insert_batch(self, keys, rets, n=None, flags=0):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_point_insert_batch(self.h, _ptr(keys), n, flags, _ptr(rets)))
+
+    def point_insert_not_exists_batch(self, keys, rets, vals, n=None, flags=0):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_point_insert_not_exists_batch(self.h, _ptr(keys), n, flags, _ptr(rets), _ptr(vals)))
+
+    def point_query_batch(self, keys, counts, n=None, flags=0, concurrent=False):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_point_query_batch(self.h, _ptr(keys), n, flags, int(concurrent), _ptr(counts)))
+
+    def serial_apply(self, hashes, op: int, n=None):
+        n = hashes.numel() if n is None else n
+        self._ok(self.L.gqf_debug_serial_apply(self.h, _ptr(hashes), n, op))
+
+    def set_stream(self, stream):
+        self._ok(self.L.gqf_set_stream(self.h, _stream_ptr(stream)))
+
+    def status(self) -> int:
+        s = _u32(0)
+        self._ok(self.L.gqf_get_status(self.h, ctypes.byref(s)))
+        return int(s.value)
+
+    def clear_status(self):
+        self._ok(self.L.gqf_clear_status(self.h))
+
+    def reset(self):
+        self._ok(self.L.gqf_reset(self.h))
+
+    def export(self) -> np.ndarray:
+        n = int(self.L.gqf_export_size(self.h))
+        out = np.zeros(n, dtype=np.uint8)
+        self._ok(self.L.gqf_export(self.h, out.ctypes.data, n))
+        return out
+
+    def import_(self, buf: np.ndarray):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self._ok(self.L.gqf_import(self.h, buf.ctypes.data, buf.size))
+
+    def profile(self, enable: bool = True):
+        self._ok(self.L.gqf_profile(self.h, int(enable)))
+
+    PHASES = ("partition", "insert", "delete", "get")
+
+    def profile_read(self) -> dict:
+        ms = np.zeros(8, dtype=np.float64)
+        calls = np.zeros(8, dtype=np.uint64)
+        keys = np.zeros(8, dtype=np.uint64)
+        self._ok(self.L.gqf_profile_read(self.h, ms.ctypes.data, calls.ctypes.data, keys.ctypes.data))
+        return {p: {"ms": float(ms[i]), "calls": int(calls[i]), "keys": int(keys[i])}
+                for i, p in enumerate(self.PHASES)}
+
+    def _ok(self, rc: int):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+
+def launch_count() -> int:
+    return int(load().gqf_launch_count())
+
+
+def exported_symbols_from_header(header: str) -> list[str]:
+    """Function names declared in include/gqf.h (for the ABI check)."""
+    import re
+
+    text = open(header).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", text, flags=re.M)
+    return sorted(set(n for n in names if n not in {"if", "while", "for", "sizeof", "defined"}))

@@ -1,0 +1,547 @@
+// Host side of the C ABI declared in include/gqf.h.
+//
+// Replaces the reference's host orchestration (src/gqf.cu:2123-2269 and
+// :3184-3419).  Differences that matter for performance:
+//   * no per-call device->host readback of num_locks and no
+//     cudaDeviceSynchronize (the reference does both on every bulk call,
+//     src/gqf.cu:3193-3201); geometry lives in a host mirror;
+//   * no per-call device allocation (thrust temporaries, managed memory):
+//     partition scratch is owned by the filter and grown stream-ordered;
+//   * the filter is built on the device (memset), not on the host and copied.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "gqf_kernels.cuh"
+#include "../../include/gqf.h"
+
+using namespace gqf;
+
+namespace gqf {
+std::atomic<unsigned long long> g_launches{0};
+}
+
+namespace {
+
+thread_local std::string g_err;
+
+void set_err(const std::string& s) { g_err = s; }
+
+bool ck(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  set_err(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+struct HostFilter {
+  QF* dqf = nullptr;        // device descriptor: the handle users hold
+  quotient_filter h{};      // host mirror of the descriptor
+  Geom g{};
+  cudaStream_t stream = 0;  // legacy default stream, like the reference
+  int log_region = 12;
+  bool auto_region = true;
+  uint8_t* aux = nullptr;   // status word + miss counter
+  Partition part{};
+  uint64_t key_cap = 0;
+  uint32_t region_cap = 0;
+  bool counts_alloc = false;
+  uint8_t* packed = nullptr;  // export / import staging
+  // phase timers (CUDA events on the launching stream), off by default
+  bool prof = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[GQF_PROF_PHASES];
+  std::vector<cudaEvent_t> spare;
+  double prof_ms[GQF_PROF_PHASES] = {0};
+  uint64_t prof_calls[GQF_PROF_PHASES] = {0};
+  uint64_t prof_keys[GQF_PROF_PHASES] = {0};
+  std::mutex mu;
+};
+
+cudaEvent_t take_event(HostFilter* f) {
+  if (!f->spare.empty()) {
+    cudaEvent_t e = f->spare.back();
+    f->spare.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets one phase of work on stream st with a pair of events.
+struct PhaseTimer {
+  HostFilter* f;
+  int phase;
+  cudaStream_t st;
+  cudaEvent_t e0 = nullptr;
+  PhaseTimer(HostFilter* f_, int ph, cudaStream_t s, uint64_t keys) : f(f_), phase(ph), st(s) {
+    if (!f->prof) return;
+    e0 = take_event(f);
+    cudaEventRecord(e0, st);
+    f->prof_calls[phase]++;
+    f->prof_keys[phase] += keys;
+  }
+  ~PhaseTimer() {
+    if (!e0) return;
+    cudaEvent_t e1 = take_event(f);
+    cudaEventRecord(e1, st);
+    f->pending[phase].push_back({e0, e1});
+  }
+};
+
+std::mutex g_mu;
+std::unordered_map<const QF*, HostFilter*> g_filters;
+
+HostFilter* lookup(const QF* qf) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_filters.find(qf);
+  if (it == g_filters.end()) {
+    set_err("unknown QF handle");
+    return nullptr;
+  }
+  return it->second;
+}
+
+int auto_log_region(int nbits) {
+  if (nbits >= 24) return 13;
+  if (nbits >= 21) return 12;
+  return 11;
+}
+
+uint32_t* status_ptr(HostFilter* f) { return reinterpret_cast<uint32_t*>(f->aux); }
+unsigned long long* misses_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 64); }
+
+uint32_t nregions_for(const HostFilter* f, int log_region) {
+  uint64_t n = f->h.nslots >> log_region;
+  return (uint32_t)(n ? n : 1);
+}
+
+// Grow partition scratch (stream-ordered, so work already queued keeps its
+// buffers until it completes).
+bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStream_t st) {
+  const uint32_t nr = nregions_for(f, f->log_region);
+  if (nkeys > 0xFFFFFFF0ULL) {
+    set_err("batch larger than 2^32 keys");
+    return false;
+  }
+  if (nkeys > f->key_cap || (with_counts && !f->counts_alloc)) {
+    uint64_t cap = nkeys > f->key_cap ? nkeys + nkeys / 8 + 1024 : f->key_cap;
+    if (f->part.keys) cudaFreeAsync(f->part.keys, st);
+    if (f->part.counts) cudaFreeAsync(f->part.counts, st);
+    f->part.keys = nullptr;
+    f->part.counts = nullptr;
+    if (!ck(cudaMallocAsync((void**)&f->part.keys, cap * sizeof(uint32_t), st), "cudaMallocAsync keys"))
+      return false;
+    if (with_counts || f->counts_alloc) {
+      if (!ck(cudaMallocAsync((void**)&f->part.counts, cap * sizeof(uint32_t), st), "cudaMallocAsync counts"))
+        return false;
+      f->counts_alloc = true;
+    }
+    f->key_cap = cap;
+  }
+  if (nr + 2 > f->region_cap) {
+    uint32_t cap = nr + 2;
+    if (f->part.region_count) cudaFreeAsync(f->part.region_count, st);
+    uint32_t* base = nullptr;
+    // region_count | region_start | cursor | deferred, one allocation
+    if (!ck(cudaMallocAsync((void**)&base, 4ULL * cap * sizeof(uint32_t), st), "cudaMallocAsync regions"))
+      return false;
+    f->part.region_count = base;
+    f->part.region_start = base + cap;
+    f->part.cursor = base + 2ULL * cap;
+    f->part.deferred = base + 3ULL * cap;
+    f->region_cap = cap;
+  }
+  f->part.nregions = nr;
+  f->part.log_region = f->log_region;
+  return true;
+}
+
+int do_bulk(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, Op op, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(f->mu);
+  if (n == 0) return 0;
+  if (!keys) {
+    set_err("null keys");
+    return -1;
+  }
+  if (!ensure_partition(f, n, false, st)) return -1;
+  Partition p = f->part;
+  p.counts = nullptr;
+  const int key_is_hash = (flags & QF_KEY_IS_HASH) ? 1 : 0;
+  {
+    PhaseTimer t(f, GQF_PROF_PARTITION, st, n);
+    if (!ck(launch_partition(f->g, p, keys, n, key_is_hash, status_ptr(f), st), "partition")) return -1;
+  }
+  {
+    PhaseTimer t(f, op == Op::kDelete ? GQF_PROF_DELETE : GQF_PROF_INSERT, st, n);
+    if (!ck(launch_rebuild(f->g, p, op, f->dqf, status_ptr(f), st), "rebuild")) return -1;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gqf_last_error(void) { return g_err.c_str(); }
+const char* gqf_version(void) { return "gqf_gb300 0.1 (sm_103a)"; }
+
+void qf_malloc_device(QF** qf, int nbits, bool bulk_config) {
+  (void)bulk_config;
+  if (!qf) return;
+  *qf = nullptr;
+  if (nbits < 6 || nbits > 36) {
+    set_err("nbits must be in [6, 36]");
+    return;
+  }
+  HostFilter* f = new HostFilter();
+  quotient_filter& h = f->h;
+  h.nslots = 1ULL << nbits;
+  // qf_init (src/gqf.cu:1950-1951): xnslots = nslots + 10 sqrt(nslots)
+  h.xnslots = h.nslots + (uint64_t)(10 * std::sqrt((double)h.nslots));
+  h.nblocks = (h.xnslots + 63) / 64;
+  h.range = h.nslots << 8;
+  h.nbits = (uint32_t)nbits;
+  h.key_bits = (uint32_t)nbits + 8;
+  h.nlocks = h.xnslots / kLockRegion + 2;  // num_locks, src/gqf.cu:1996
+  h.lock_spin_limit = 1u << 20;
+  bool ok = ck(cudaMalloc((void**)&h.blocks, h.nblocks * sizeof(Block)), "cudaMalloc blocks") &&
+            ck(cudaMemset(h.blocks, 0, h.nblocks * sizeof(Block)), "cudaMemset blocks") &&
+            ck(cudaMalloc((void**)&h.locks, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMalloc locks") &&
+            ck(cudaMemset(h.locks, 0, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMemset locks") &&
+            ck(cudaMalloc((void**)&f->aux, 256), "cudaMalloc aux") &&
+            ck(cudaMemset(f->aux, 0, 256), "cudaMemset aux");
+  if (ok) {
+    h.status = status_ptr(f);
+    ok = ck(cudaMalloc((void**)&f->dqf, sizeof(quotient_filter)), "cudaMalloc descriptor") &&
+         ck(cudaMemcpy(f->dqf, &h, sizeof(quotient_filter), cudaMemcpyHostToDevice), "cudaMemcpy descriptor");
+  }
+  if (!ok) {
+    if (h.blocks) cudaFree(h.blocks);
+    if (h.locks) cudaFree(h.locks);
+    if (f->aux) cudaFree(f->aux);
+    if (f->dqf) cudaFree(f->dqf);
+    delete f;
+    return;
+  }
+  f->g.blocks = h.blocks;
+  f->g.nslots = h.nslots;
+  f->g.xnslots = h.xnslots;
+  f->g.nblocks = h.nblocks;
+  f->g.range = h.range;
+  f->g.mask = h.range - 1;
+  f->g.nbits = h.nbits;
+  f->log_region = auto_log_region(nbits);
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_filters[f->dqf] = f;
+  }
+  *qf = f->dqf;
+}
+
+void qf_destroy_device(QF* qf) {
+  HostFilter* f = lookup(qf);
+  if (!f) return;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_filters.erase(qf);
+  }
+  cudaStreamSynchronize(f->stream);
+  cudaDeviceSynchronize();
+  for (auto& v : f->pending)
+    for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+  for (cudaEvent_t e : f->spare) cudaEventDestroy(e);
+  if (f->part.keys) cudaFree(f->part.keys);
+  if (f->part.counts) cudaFree(f->part.counts);
+  if (f->part.region_count) cudaFree(f->part.region_count);
+  if (f->packed) cudaFree(f->packed);
+  cudaFree(f->h.blocks);
+  cudaFree(f->h.locks);
+  cudaFree(f->aux);
+  cudaFree(f->dqf);
+  delete f;
+}
+
+void bulk_insert(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
+  if (HostFilter* f = lookup(qf)) do_bulk(f, nvals, keys, flags, Op::kInsert, f->stream);
+}
+
+// Duplicates inside a batch are merged into counters by the rebuild itself,
+// so the reduce variant needs no separate sort + reduce_by_key
+// (src/gqf.cu:3261-3279).
+void bulk_insert_reduce(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
+  if (HostFilter* f = lookup(qf)) do_bulk(f, nvals, keys, flags, Op::kInsert, f->stream);
+}
+
+void bulk_delete(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
+  if (HostFilter* f = lookup(qf)) do_bulk(f, nvals, keys, flags, Op::kDelete, f->stream);
+}
+
+void bulk_get(QF* qf, uint64_t nvals, uint64_t* vals, uint64_t* returns) {
+  HostFilter* f = lookup(qf);
+  if (!f) return;
+  std::lock_guard<std::mutex> lk(f->mu);
+  PhaseTimer t(f, GQF_PROF_GET, f->stream, nvals);
+  ck(launch_bulk_get(f->g, vals, nvals, returns, 0, f->stream), "bulk_get");
+}
+
+uint64_t bulk_get_misses_wrapper(QF* qf, uint64_t* vals, uint64_t nvals) {
+  HostFilter* f = lookup(qf);
+  if (!f) return 0;
+  std::lock_guard<std::mutex> lk(f->mu);
+  unsigned long long m = 0;
+  if (ck(cudaMemsetAsync(misses_ptr(f), 0, 8, f->stream), "memset") &&
+      ck(launch_bulk_get_misses(f->g, vals, nvals, misses_ptr(f), f->stream), "bulk_get_misses") &&
+      ck(cudaMemcpyAsync(&m, misses_ptr(f), 8, cudaMemcpyDeviceToHost, f->stream), "memcpy") &&
+      ck(cudaStreamSynchronize(f->stream), "sync"))
+    return m;
+  return 0;
+}
+
+uint64_t point_get_wrapper(QF* qf, uint64_t* hashes, uint64_t nitems) {
+  HostFilter* f = lookup(qf);
+  if (!f) return 0;
+  std::lock_guard<std::mutex> lk(f->mu);
+  unsigned long long m = 0;
+  if (ck(cudaMemsetAsync(misses_ptr(f), 0, 8, f->stream), "memset") &&
+      ck(launch_point_get_misses(f->dqf, hashes, nitems, misses_ptr(f), f->stream), "point_get") &&
+      ck(cudaMemcpyAsync(&m, misses_ptr(f), 8, cudaMemcpyDeviceToHost, f->stream), "memcpy") &&
+      ck(cudaStreamSynchronize(f->stream), "sync"))
+    return m;
+  return 0;
+}
+
+int gqf_point_bulk_insert(QF* qf, uint64_t* keys, uint64_t nitems) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(launch_point_bulk_insert(f->dqf, keys, nitems, f->stream), "point_bulk_insert") ? 0 : -1;
+}
+
+int gqf_point_insert_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags, int8_t* rets) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(launch_point_insert(f->dqf, keys, n, flags, rets, f->stream), "point_insert") ? 0 : -1;
+}
+
+int gqf_point_insert_not_exists_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags,
+                                      int8_t* rets, uint8_t* vals) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(launch_point_insert_not_exists(f->dqf, keys, n, flags, rets, vals, f->stream),
+            "point_insert_not_exists") ? 0 : -1;
+}
+
+int gqf_point_query_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags, int concurrent,
+                          uint64_t* counts) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(launch_point_query(f->dqf, keys, n, flags, concurrent, counts, f->stream), "point_query") ? 0 : -1;
+}
+
+int gqf_bulk_insert_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream) {
+  HostFilter* f = lookup(qf);
+  return f ? do_bulk(f, nvals, keys, flags, Op::kInsert, (cudaStream_t)stream) : -1;
+}
+
+int gqf_bulk_insert_reduce_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags,
+                                 void* stream) {
+  HostFilter* f = lookup(qf);
+  return f ? do_bulk(f, nvals, keys, flags, Op::kInsert, (cudaStream_t)stream) : -1;
+}
+
+int gqf_bulk_delete_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream) {
+  HostFilter* f = lookup(qf);
+  return f ? do_bulk(f, nvals, keys, flags, Op::kDelete, (cudaStream_t)stream) : -1;
+}
+
+int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* returns, uint8_t flags,
+                       void* stream) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  PhaseTimer t(f, GQF_PROF_GET, (cudaStream_t)stream, nvals);
+  return ck(launch_bulk_get(f->g, vals, nvals, returns, (flags & QF_KEY_IS_HASH) ? 1 : 0,
+                            (cudaStream_t)stream), "bulk_get") ? 0 : -1;
+}
+
+int gqf_set_stream(QF* qf, void* stream) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  f->stream = (cudaStream_t)stream;
+  return 0;
+}
+
+int gqf_set_region_log(QF* qf, int log_region) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  if (log_region == 0) {
+    f->auto_region = true;
+    f->log_region = auto_log_region((int)f->h.nbits);
+    return 0;
+  }
+  if (log_region < kMinLogRegion || log_region > kMaxLogRegion) {
+    set_err("log_region must be 11, 12 or 13");
+    return -1;
+  }
+  f->auto_region = false;
+  f->log_region = log_region;
+  return 0;
+}
+
+int gqf_get_region_log(QF* qf) {
+  HostFilter* f = lookup(qf);
+  return f ? f->log_region : -1;
+}
+
+uint64_t gqf_nslots(QF* qf) { HostFilter* f = lookup(qf); return f ? f->h.nslots : 0; }
+uint64_t gqf_xnslots(QF* qf) { HostFilter* f = lookup(qf); return f ? f->h.xnslots : 0; }
+uint64_t gqf_nblocks(QF* qf) { HostFilter* f = lookup(qf); return f ? f->h.nblocks : 0; }
+uint64_t gqf_device_bytes(QF* qf) {
+  HostFilter* f = lookup(qf);
+  return f ? f->h.nblocks * sizeof(Block) : 0;
+}
+
+int gqf_get_status(QF* qf, uint32_t* status) {
+  HostFilter* f = lookup(qf);
+  if (!f || !status) return -1;
+  uint32_t s = 0;
+  if (!ck(cudaMemcpyAsync(&s, status_ptr(f), 4, cudaMemcpyDeviceToHost, f->stream), "memcpy status") ||
+      !ck(cudaStreamSynchronize(f->stream), "sync"))
+    return -1;
+  *status = s;
+  return 0;
+}
+
+int gqf_clear_status(QF* qf) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(cudaMemsetAsync(status_ptr(f), 0, 4, f->stream), "memset status") ? 0 : -1;
+}
+
+int gqf_reset(QF* qf) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(cudaMemsetAsync(f->h.blocks, 0, f->h.nblocks * sizeof(Block), f->stream), "memset blocks") ? 0 : -1;
+}
+
+uint64_t gqf_export_size(QF* qf) {
+  HostFilter* f = lookup(qf);
+  return f ? 120 + f->h.nblocks * 81 : 0;
+}
+
+namespace {
+// qfmetadata (include/gqf_int.cuh:96-113) as qf_init fills it for
+// qf_malloc_device's parameters (src/gqf.cu:1978-1994); the element counters
+// stay 0, as in the reference, which never updates them on the device.
+void fill_metadata(const HostFilter* f, uint8_t* out) {
+  uint64_t w[15] = {0};
+  w[0] = 1018874902021329732ULL;            // MAGIC_NUMBER
+  w[1] = (uint64_t)QF_HASH_INVERTIBLE;      // hash_mode (int) | reserved (0)
+  w[2] = f->h.nblocks * 81;                 // total_size_in_bytes
+  w[3] = 0;                                 // seed | padding
+  w[4] = f->h.nslots;
+  w[5] = f->h.xnslots;
+  w[6] = f->h.key_bits;
+  w[7] = 0;                                 // value_bits
+  w[8] = 8;                                 // key_remainder_bits
+  w[9] = 8;                                 // bits_per_slot
+  w[10] = f->h.range;
+  w[11] = f->h.nblocks;
+  std::memcpy(out, w, 120);
+}
+
+bool ensure_packed(HostFilter* f) {
+  if (f->packed) return true;
+  return ck(cudaMalloc((void**)&f->packed, f->h.nblocks * 81), "cudaMalloc packed");
+}
+}  // namespace
+
+int gqf_export(QF* qf, void* host_buf, uint64_t len) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  uint64_t need = 120 + f->h.nblocks * 81;
+  if (!host_buf || len < need) {
+    set_err("export buffer too small");
+    return -1;
+  }
+  if (!ensure_packed(f)) return -1;
+  uint8_t* out = static_cast<uint8_t*>(host_buf);
+  fill_metadata(f, out);
+  if (!ck(launch_export(f->g, f->packed, f->stream), "export") ||
+      !ck(cudaMemcpyAsync(out + 120, f->packed, f->h.nblocks * 81, cudaMemcpyDeviceToHost, f->stream), "memcpy") ||
+      !ck(cudaStreamSynchronize(f->stream), "sync"))
+    return -1;
+  return 0;
+}
+
+int gqf_import(QF* qf, const void* host_buf, uint64_t len) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  uint64_t need = 120 + f->h.nblocks * 81;
+  if (!host_buf || len != need) {
+    set_err("import image size does not match this filter");
+    return -1;
+  }
+  uint8_t meta[120];
+  fill_metadata(f, meta);
+  const uint8_t* in = static_cast<const uint8_t*>(host_buf);
+  // nslots, xnslots, key_bits, nblocks must agree
+  if (std::memcmp(in + 32, meta + 32, 24) != 0 || std::memcmp(in + 88, meta + 88, 8) != 0) {
+    set_err("import image geometry does not match this filter");
+    return -1;
+  }
+  if (!ensure_packed(f)) return -1;
+  if (!ck(cudaMemcpyAsync(f->packed, in + 120, f->h.nblocks * 81, cudaMemcpyHostToDevice, f->stream), "memcpy") ||
+      !ck(launch_import(f->g, f->packed, f->stream), "import") ||
+      !ck(launch_import_fix(f->dqf, f->packed, f->stream), "import_fix") ||
+      !ck(cudaStreamSynchronize(f->stream), "sync"))
+    return -1;
+  return 0;
+}
+
+int gqf_profile(QF* qf, int enable) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  f->prof = enable != 0;
+  for (int i = 0; i < GQF_PROF_PHASES; i++) { f->prof_ms[i] = 0; f->prof_calls[i] = 0; f->prof_keys[i] = 0; }
+  return 0;
+}
+
+int gqf_profile_read(QF* qf, double* ms, uint64_t* calls, uint64_t* keys) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  for (int i = 0; i < GQF_PROF_PHASES; i++) {
+    for (auto& pr : f->pending[i]) {
+      float t = 0;
+      if (!ck(cudaEventSynchronize(pr.second), "event sync")) return -1;
+      cudaEventElapsedTime(&t, pr.first, pr.second);
+      f->prof_ms[i] += t;
+      f->spare.push_back(pr.first);
+      f->spare.push_back(pr.second);
+    }
+    f->pending[i].clear();
+    if (ms) ms[i] = f->prof_ms[i];
+    if (calls) calls[i] = f->prof_calls[i];
+    if (keys) keys[i] = f->prof_keys[i];
+  }
+  return 0;
+}
+
+uint64_t gqf_launch_count(void) { return g_launches.load(); }
+
+int gqf_debug_serial_apply(QF* qf, const uint64_t* hashes, uint64_t n, int op) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  return ck(launch_serial_apply(f->dqf, hashes, n, op, f->stream), "serial_apply") ? 0 : -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// Kernel entry points of the GB300 GQF and the host-side launchers that the
+// C ABI (gqf_api.cu) calls.  Every launcher enqueues on the given stream and
+// returns the launch error, never synchronising.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "gqf_device.cuh"
+
+namespace gqf {
+
+// Kernels launched by this library since load (every <<<>>> counts one).
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Geometry of one filter as passed by value to kernels.
+struct Geom {
+  Block* blocks;
+  uint64_t nslots, xnslots, nblocks;
+  uint64_t range;   // 2^(nbits+8)
+  uint64_t mask;    // range - 1
+  uint32_t nbits;
+};
+
+// Scratch the bulk path partitions keys into.  Owned by the filter, grown on
+// demand by the host (gqf_api.cu).
+struct Partition {
+  uint32_t* keys;          // region-local hashes, grouped by region
+  uint32_t* counts;        // per-key multiplicities, or nullptr (all 1)
+  uint32_t* region_count;  // nregions + 1
+  uint32_t* region_start;  // nregions + 1 (exclusive prefix)
+  uint32_t* cursor;        // nregions
+  uint32_t* deferred;      // [0] = n, then region ids
+  uint32_t nregions;
+  int log_region;          // a region is 2^log_region quotients
+};
+
+enum class Op : int { kInsert = 0, kDelete = 1 };
+
+// Region sizes the rebuild kernel is instantiated for.
+constexpr int kMinLogRegion = 11;
+constexpr int kMaxLogRegion = 13;
+
+cudaError_t launch_bulk_get(const Geom& g, const uint64_t* keys, uint64_t n, uint64_t* out,
+                            int key_is_hash, cudaStream_t st);
+cudaError_t launch_bulk_get_misses(const Geom& g, const uint64_t* keys, uint64_t n,
+                                   unsigned long long* misses, cudaStream_t st);
+
+// hash -> per-region counts -> prefix -> scatter of region-local hashes.
+cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
+                             int key_is_hash, uint32_t* status, cudaStream_t st);
+
+// Even regions, then odd regions, then the serial fallback for regions whose
+// rebuild window was exceeded.
+cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_filter* dqf,
+                           uint32_t* status, cudaStream_t st);
+size_t rebuild_smem_bytes(int log_region);
+
+cudaError_t launch_export(const Geom& g, uint8_t* packed, cudaStream_t st);
+cudaError_t launch_import(const Geom& g, const uint8_t* packed, cudaStream_t st);
+cudaError_t launch_import_fix(quotient_filter* dqf, const uint8_t* packed, cudaStream_t st);
+
+// Point-API batch kernels (one thread per key).
+cudaError_t launch_point_insert(quotient_filter* dqf, const uint64_t* keys, uint64_t n, uint8_t flags,
+                                int8_t* rets, cudaStream_t st);
+cudaError_t launch_point_insert_not_exists(quotient_filter* dqf, const uint64_t* keys, uint64_t n,
+                                           uint8_t flags, int8_t* rets, uint8_t* vals,
+                                           cudaStream_t st);
+cudaError_t launch_point_query(quotient_filter* dqf, const uint64_t* keys, uint64_t n, uint8_t flags,
+                               int concurrent, uint64_t* counts, cudaStream_t st);
+cudaError_t launch_point_get_misses(quotient_filter* dqf, const uint64_t* keys, uint64_t n,
+                                    unsigned long long* misses, cudaStream_t st);
+cudaError_t launch_point_bulk_insert(quotient_filter* dqf, uint64_t* keys, uint64_t n, cudaStream_t st);
+cudaError_t launch_serial_apply(quotient_filter* dqf, const uint64_t* hashes, uint64_t n, int op,
+                                cudaStream_t st);
+
+}  // namespace gqf

@@ -1,0 +1,140 @@
+// Hash + partition of a key batch by region (a radix partition on the top
+// quotient bits).  Replaces the reference's hash_all + thrust::sort +
+// set_buffers_binary + set_buffer_lens (src/gqf.cu:2615-2750, :3206-3215):
+// only the region of each hash matters for the even/odd schedule, and the
+// rebuild kernel sorts each region's keys in shared memory.
+//
+// Pass 1 counts keys per region, pass 2 scans the counts, pass 3 scatters
+// each key's region-local hash (low 8 + log_region bits, a uint32) into its
+// region's bucket.  Same-region keys inside a warp share one atomic
+// (match.any), which keeps skewed batches from serialising on hot regions.
+#include "gqf_kernels.cuh"
+
+namespace gqf {
+namespace {
+
+__device__ __forceinline__ bool hash_key(const Geom& g, const uint64_t* keys, uint64_t i, uint64_t n,
+                                         int key_is_hash, uint32_t* status, uint64_t* h) {
+  if (i >= n) return false;
+  uint64_t k = keys[i];
+  if (key_is_hash) {
+    if (k >= g.range) {
+      if (status) atomicOr(status, kStBadKey);
+      return false;
+    }
+    *h = k;
+  } else {
+    *h = hash64(k, g.mask);
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(256) k_part_count(Geom g, const uint64_t* __restrict__ keys,
+                                                    uint64_t n, int key_is_hash, int shift,
+                                                    uint32_t* __restrict__ region_count,
+                                                    uint32_t* status) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t nr = (n + 31) & ~31ULL;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nr; i += stride) {
+    uint64_t h = 0;
+    bool ok = hash_key(g, keys, i, n, key_is_hash, status, &h);
+    uint32_t r = ok ? (uint32_t)(h >> shift) : 0xFFFFFFFFu;
+    unsigned peers = __match_any_sync(0xffffffffu, r);
+    if (ok && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&region_count[r], (uint32_t)__popc(peers));
+  }
+}
+
+// Exclusive scan of nregions counts by one CTA; also resets the cursors.
+__global__ void __launch_bounds__(1024) k_part_scan(const uint32_t* __restrict__ region_count,
+                                                    uint32_t* __restrict__ region_start,
+                                                    uint32_t* __restrict__ cursor, uint32_t nregions) {
+  __shared__ uint32_t warp_sum[32];
+  const uint32_t per = (nregions + blockDim.x - 1) / blockDim.x;
+  const uint32_t a = threadIdx.x * per;
+  const uint32_t b = min(a + per, nregions);
+  uint32_t s = 0;
+  for (uint32_t i = a; i < b; i++) s += region_count[i];
+  // block exclusive scan of s
+  uint32_t v = s;
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= (unsigned)o) v += t;
+  }
+  if (lane == 31) warp_sum[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = lane < (blockDim.x >> 5) ? warp_sum[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= (unsigned)o) w += t;
+    }
+    warp_sum[lane] = w;
+  }
+  __syncthreads();
+  uint32_t excl = v - s + (wid ? warp_sum[wid - 1] : 0);
+  for (uint32_t i = a; i < b; i++) {
+    region_start[i] = excl;
+    cursor[i] = excl;
+    excl += region_count[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) region_start[nregions] = excl;
+}
+
+__global__ void __launch_bounds__(256) k_part_scatter(Geom g, const uint64_t* __restrict__ keys,
+                                                      uint64_t n, int key_is_hash, int shift,
+                                                      uint32_t* __restrict__ cursor,
+                                                      uint32_t* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t nr = (n + 31) & ~31ULL;
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t local_mask = (1ULL << shift) - 1ULL;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nr; i += stride) {
+    uint64_t h = 0;
+    bool ok = hash_key(g, keys, i, n, key_is_hash, nullptr, &h);
+    uint32_t r = ok ? (uint32_t)(h >> shift) : 0xFFFFFFFFu;
+    unsigned peers = __match_any_sync(0xffffffffu, r);
+    unsigned leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (ok && lane == leader) base = atomicAdd(&cursor[r], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (ok) out[base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)(h & local_mask);
+  }
+}
+
+int grid_for(uint64_t n) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  uint64_t want = (n + 255) / 256;
+  uint64_t cap = (uint64_t)sms * 16;
+  if (want > cap) want = cap;
+  return (int)(want ? want : 1);
+}
+
+}  // namespace
+
+cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
+                             int key_is_hash, uint32_t* status, cudaStream_t st) {
+  const int shift = 8 + p.log_region;
+  cudaError_t e = cudaMemsetAsync(p.region_count, 0, (p.nregions + 1) * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (n) {
+    k_part_count<<<grid_for(n), 256, 0, st>>>(g, keys, n, key_is_hash, shift, p.region_count, status);
+    count_launch();
+  }
+  k_part_scan<<<1, 1024, 0, st>>>(p.region_count, p.region_start, p.cursor, p.nregions);
+  count_launch();
+  if (n) {
+    k_part_scatter<<<grid_for(n), 256, 0, st>>>(g, keys, n, key_is_hash, shift, p.cursor, p.keys);
+    count_launch();
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace gqf

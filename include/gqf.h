@@ -1,0 +1,182 @@
+/*
+ * gqf.h -- C ABI of the GB300 counting quotient filter (libgqf_gb300.so).
+ *
+ * Drop-in for the host half of PASSIONLab/cqf's GQF API (include/gqf.cuh of
+ * the reference, whose extern "C" block opens at include/gqf.cuh:19).  Every
+ * entry point below names the reference declaration it replaces.  Plain C:
+ * pointers, sizes and integers only, so it binds from C, C++, cgo, ctypes or
+ * JNI without CUDA headers.  Device pointers are passed as ordinary pointers.
+ *
+ * Semantics kept from the reference:
+ *   - qf_malloc_device returns a DEVICE pointer to the filter descriptor; the
+ *     host must not dereference it (src/gqf.cu:2212-2217).
+ *   - Keys are 64-bit; with QF_KEY_IS_HASH clear they are hashed with the
+ *     reference's invertible hash_64 under 2^(nbits+8)-1, so two keys that
+ *     agree modulo 2^(nbits+8) are the same key (src/hashutil.cu:132).
+ *   - Bulk calls are asynchronous on the filter's stream (the legacy default
+ *     stream unless gqf_set_stream is called), like the reference's.
+ *   - The layout after any sequence of calls is word-for-word the reference's
+ *     (gqf_export gives the reference's packed bytes).
+ *
+ * Differences, all documented at the entry points:
+ *   - bulk_insert / bulk_insert_reduce / bulk_delete leave `keys` unmodified
+ *     (the reference overwrote them with sorted hashes, src/gqf.cu:3206-3209;
+ *     every caller in the reference regenerates keys afterwards).
+ *   - Failures never print, assert or trap on the device: they accumulate in
+ *     a status word read with gqf_get_status.
+ */
+#ifndef GQF_GB300_H
+#define GQF_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* include/gqf.cuh:22-23 */
+typedef struct quotient_filter quotient_filter;
+typedef quotient_filter QF;
+
+/* include/gqf.cuh:45-49 */
+enum qf_hashmode { QF_HASH_DEFAULT, QF_HASH_INVERTIBLE, QF_HASH_NONE };
+
+/* include/gqf.cuh:52-56; QF_TIMEOUT is new: a bounded lock wait gave up. */
+enum qf_returns { QF_ITEM_INSERTED, QF_ITEM_FOUND, QF_FULL, QF_TIMEOUT };
+
+/* include/gqf.cuh:74-80 */
+#define QF_NO_LOCK (0x01)
+#define QF_TRY_ONCE_LOCK (0x02)
+#define QF_WAIT_FOR_LOCK (0x04)
+#define QF_KEY_IS_HASH (0x08)
+
+/* include/gqf.cuh:213-215 */
+#define QF_NO_SPACE (-1)
+#define QF_COULDNT_LOCK (-2)
+#define QF_DOESNT_EXIST (-3)
+
+/* Status bits returned by gqf_get_status. */
+#define GQF_STATUS_FULL (1u << 0)     /* an insert found no free slot (keys dropped) */
+#define GQF_STATUS_TIMEOUT (1u << 1)  /* a bounded device wait gave up */
+#define GQF_STATUS_BAD_KEY (1u << 2)  /* a QF_KEY_IS_HASH key >= 2^(nbits+8) was skipped */
+#define GQF_STATUS_DEFERRED (1u << 3) /* a region took the serial path (informational) */
+#define GQF_STATUS_OVERFLOW (1u << 4) /* an internal limit was exceeded */
+
+/* ----------------------------------------------------------- reference API */
+
+/* include/gqf.cuh:87.  2^nbits slots, 8-bit remainders.  bulk_config is
+ * accepted for compatibility; both the bulk and the point paths are ready.
+ * On failure *qf is set to NULL and gqf_last_error() says why. */
+void qf_malloc_device(QF** qf, int nbits, bool bulk_config);
+
+/* include/gqf.cuh:88 */
+void qf_destroy_device(QF* qf);
+
+/* include/gqf.cuh:109.  Inserts nvals device-resident keys (count 1 each). */
+void bulk_insert(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags);
+
+/* include/gqf.cuh:112.  Same result as bulk_insert; for skewed batches. */
+void bulk_insert_reduce(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags);
+
+/* include/gqf.cuh:115.  Decrements each key's count by one (absent keys are
+ * ignored; a count reaching 0 removes the key). */
+void bulk_delete(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags);
+
+/* include/gqf.cuh:118.  returns[i] = count of vals[i] (0 if absent). */
+void bulk_get(QF* qf, uint64_t nvals, uint64_t* vals, uint64_t* returns);
+
+/* include/gqf.cuh:136.  Number of vals with count < 1; synchronises. */
+uint64_t bulk_get_misses_wrapper(QF* qf, uint64_t* vals, uint64_t nvals);
+
+/* include/gqf.cuh:128.  Point-API lookups of nitems keys; returns the number
+ * not found; synchronises. */
+uint64_t point_get_wrapper(QF* qf, uint64_t* hashes, uint64_t nitems);
+
+/* ------------------------------------------------------------- extensions */
+
+/* Host launcher for the reference's point_bulk_insert kernel
+ * (include/gqf.cuh:130, src/gqf.cu:3153): point_insert per key, keys hashed. */
+int gqf_point_bulk_insert(QF* qf, uint64_t* keys, uint64_t nitems);
+
+/* Batched point-API calls, one device thread per key (the reference's
+ * point_insert / point_insert_not_exists / point_query(_concurrent),
+ * include/gqf.cuh:94-103).  rets / vals / counts are device arrays. */
+int gqf_point_insert_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags, int8_t* rets);
+int gqf_point_insert_not_exists_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags,
+                                      int8_t* rets, uint8_t* vals);
+int gqf_point_query_batch(QF* qf, const uint64_t* keys, uint64_t n, uint8_t flags, int concurrent,
+                          uint64_t* counts);
+
+/* Asynchronous bulk calls with an explicit CUDA stream (cudaStream_t passed
+ * as void*; NULL = legacy default stream).  The plain entry points above use
+ * the filter's stream. */
+int gqf_bulk_insert_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
+int gqf_bulk_insert_reduce_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags,
+                                 void* stream);
+int gqf_bulk_delete_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
+int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* returns, uint8_t flags,
+                       void* stream);
+
+/* The filter's default stream for the reference entry points. */
+int gqf_set_stream(QF* qf, void* stream);
+
+/* Region size of the bulk rebuild: 2^log_region quotients (11, 12 or 13).
+ * Does not change results, only speed; 0 restores the automatic choice. */
+int gqf_set_region_log(QF* qf, int log_region);
+int gqf_get_region_log(QF* qf);
+
+/* Geometry: 2^nbits slots, xnslots = nslots + 10 sqrt(nslots) slots in
+ * 64-slot blocks (qf_init, src/gqf.cu:1939-1996). */
+uint64_t gqf_nslots(QF* qf);
+uint64_t gqf_xnslots(QF* qf);
+uint64_t gqf_nblocks(QF* qf);
+/* Device bytes held by the filter's blocks. */
+uint64_t gqf_device_bytes(QF* qf);
+
+/* Status word (GQF_STATUS_*) accumulated since the last clear; synchronises
+ * the filter's stream.  Returns 0 on success, nonzero on a CUDA error. */
+int gqf_get_status(QF* qf, uint32_t* status);
+int gqf_clear_status(QF* qf);
+
+/* Empty the filter (asynchronous). */
+int gqf_reset(QF* qf);
+
+/* The reference's packed format: the 120-byte qfmetadata header then nblocks
+ * 81-byte qfblocks (include/gqf_int.cuh:38-113), exactly the buffer the
+ * reference's filter would hold after the same operations.  export_size is
+ * the byte count; export writes to a host buffer and synchronises. */
+uint64_t gqf_export_size(QF* qf);
+int gqf_export(QF* qf, void* host_buf, uint64_t len);
+/* Load a packed image (same nbits) into the filter; synchronises. */
+int gqf_import(QF* qf, const void* host_buf, uint64_t len);
+
+/* Phase timers: with profiling on, every bulk call brackets its phases with
+ * CUDA events on its stream.  gqf_profile_read synchronises and returns, per
+ * phase, the summed device milliseconds, the number of calls and the keys
+ * processed since profiling was enabled (arrays of GQF_PROF_PHASES). */
+#define GQF_PROF_PARTITION 0 /* hash + radix partition by region */
+#define GQF_PROF_INSERT 1    /* region rebuild for inserts (both phases + fallback) */
+#define GQF_PROF_DELETE 2    /* region rebuild for deletes */
+#define GQF_PROF_GET 3       /* probe kernel */
+#define GQF_PROF_PHASES 8
+int gqf_profile(QF* qf, int enable);
+int gqf_profile_read(QF* qf, double* ms, uint64_t* calls, uint64_t* keys);
+
+/* Kernels launched by the library since it was loaded (all filters). */
+uint64_t gqf_launch_count(void);
+
+/* Testing support: apply hashes one at a time with the reference's
+ * single-key algorithms on the device (op 0 insert count 1, 1 remove one). */
+int gqf_debug_serial_apply(QF* qf, const uint64_t* hashes, uint64_t n, int op);
+
+/* Last host-side error message of the calling thread ("" if none). */
+const char* gqf_last_error(void);
+
+/* Library version string. */
+const char* gqf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GQF_GB300_H */

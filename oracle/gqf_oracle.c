@@ -11,9 +11,10 @@
  *  - bitselect is a portable binary search instead of x86 pdep/tzcnt
  *    (src/gqf.cu:496-507); both return the position of the rank-th set bit,
  *    or 64.
- *  - Slot reads past the allocated blocks return 0 and walks past the last
- *    block stop, where the reference asserts or reads out of bounds
- *    (src/gqf.cu:535, :728-770, :1172-1190).
+ *  - Slot reads past the allocated blocks return 0 and every walk stops at
+ *    the end of the table, where the reference asserts, reads out of bounds
+ *    or loops forever (src/gqf.cu:535, :728-770, :1133-1190, :1326-1334,
+ *    :1660-1661); only tables pushed past full reach these states.
  *  - The metadata counters nelts / ndistinct_elts / noccupied_slots stay 0,
  *    as they do in the reference (every modify_metadata is commented out).
  */
@@ -471,7 +472,7 @@ static int remove_replace_slots(oqf* qf, int operation, uint64_t bucket_index,
   uint64_t current_distance = old_length - total_remainders;
   int ret_current_distance = (int)current_distance;
 
-  while (current_distance > 0) {
+  while (current_distance > 0 && current_slot + current_distance <= SPB * qf->nblocks) {
     if (is_runend(qf, current_slot + current_distance - 1)) {
       do {
         current_bucket++;
@@ -601,7 +602,7 @@ static uint64_t decode_counter(const oqf* qf, uint64_t index, uint64_t* remainde
   cnt = 0;
   base = (1ULL << 8) - (rem ? 2 : 1);
   end = index + 1;
-  while (digit != rem && !is_runend(qf, end)) {
+  while (digit != rem && !is_runend(qf, end) && end + 1 < SPB * qf->nblocks) {
     if (digit > rem) digit--;
     if (digit && rem) digit--;
     cnt = cnt * base + digit;
@@ -762,7 +763,8 @@ static int insert1(oqf* qf, uint64_t hash) {
       new_value = 1;
     } else {
       insert_index = runstart_index + 1;
-      while (get_slot(qf, insert_index + 1) != hash_remainder) insert_index++;
+      while (get_slot(qf, insert_index + 1) != hash_remainder && insert_index + 1 < SPB * qf->nblocks)
+        insert_index++;
       uint64_t digit, carry;
       do {
         carry = 0;
@@ -852,7 +854,8 @@ static int insert_count(oqf* qf, uint64_t hash, uint64_t count) {
     } else {
       uint64_t current_remainder, current_count, current_end;
       current_end = decode_counter(qf, runstart_index, &current_remainder, &current_count);
-      while (current_remainder < hash_remainder && !is_runend(qf, current_end)) {
+      while (current_remainder < hash_remainder && !is_runend(qf, current_end) &&
+             current_end + 1 < SPB * qf->nblocks) {
         runstart_index = current_end + 1;
         current_end = decode_counter(qf, runstart_index, &current_remainder, &current_count);
       }
@@ -896,7 +899,8 @@ static int remove_count(oqf* qf, uint64_t hash, uint64_t count) {
   int only_item_in_the_run = 0;
 
   current_end = decode_counter(qf, runstart_index, &current_remainder, &current_count);
-  while (current_remainder < hash_remainder && !is_runend(qf, current_end)) {
+  while (current_remainder < hash_remainder && !is_runend(qf, current_end) &&
+         current_end + 1 < SPB * qf->nblocks) {
     runstart_index = current_end + 1;
     current_end = decode_counter(qf, runstart_index, &current_remainder, &current_count);
   }
@@ -937,7 +941,7 @@ uint64_t oqf_count(const oqf* qf, uint64_t hash) {
     current_end = decode_counter(qf, runstart_index, &current_remainder, &current_count);
     if (current_remainder == hash_remainder) return current_count;
     runstart_index = current_end + 1;
-  } while (!is_runend(qf, current_end));
+  } while (!is_runend(qf, current_end) && (uint64_t)runstart_index < SPB * qf->nblocks);
   return 0;
 }
 
@@ -961,7 +965,7 @@ uint64_t oqf_query(const oqf* qf, uint64_t hash, uint64_t* value) {
     *value = 0; /* current_remainder & BITMASK(value_bits = 0) */
     if (current_remainder == hash_remainder) return current_count;
     runstart_index = current_end + 1;
-  } while (!is_runend(qf, current_end));
+  } while (!is_runend(qf, current_end) && (uint64_t)runstart_index < SPB * qf->nblocks);
   return 0;
 }
 
