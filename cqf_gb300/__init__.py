@@ -56,6 +56,7 @@ SIGNATURES = {
     "gqf_bulk_insert_reduce_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_delete_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_get_async": (_int, [_vp, _u64, _vp, _vp, _u8, _vp]),
+    "gqf_bulk_insert_noalloc": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
@@ -203,6 +204,11 @@ class QF:
     # ---- extensions
     def bulk_insert_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
         self._ok(self.L.gqf_bulk_insert_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
+
+    def bulk_insert_noalloc(self, keys, n=None, flags=QF_NO_LOCK, stream=None):
+        """bulk_insert that allocates nothing (fixed scratch; see include/gqf.h)."""
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_bulk_insert_noalloc(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
 
     def bulk_delete_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
         self._ok(self.L.gqf_bulk_delete_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))

@@ -185,6 +185,25 @@ int do_bulk(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, Op o
 
 }  // namespace
 
+namespace gqf {
+// Read-only view of a filter for entry points defined in other translation
+// units of this library.
+bool internal_view(const QF* qf, FilterView* v) {
+  HostFilter* f = lookup(qf);
+  if (!f) return false;
+  v->g = f->g;
+  v->dqf = f->dqf;
+  v->status = status_ptr(f);
+  v->log_region = f->log_region;
+  v->nregions = nregions_for(f, f->log_region);
+  v->stream = f->stream;
+  v->mu = &f->mu;
+  return true;
+}
+
+void internal_set_error(const char* msg) { set_err(msg); }
+}  // namespace gqf
+
 extern "C" {
 
 const char* gqf_last_error(void) { return g_err.c_str(); }

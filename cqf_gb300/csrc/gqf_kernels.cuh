@@ -38,6 +38,19 @@ struct Partition {
 
 enum class Op : int { kInsert = 0, kDelete = 1 };
 
+// What other translation units of the library may see of a filter.
+struct FilterView {
+  Geom g;
+  quotient_filter* dqf;
+  uint32_t* status;
+  int log_region;
+  uint32_t nregions;
+  cudaStream_t stream;
+  void* mu;  // std::mutex* serialising calls on the filter
+};
+bool internal_view(const quotient_filter* qf, FilterView* v);
+void internal_set_error(const char* msg);
+
 // Region sizes the rebuild kernel is instantiated for.
 constexpr int kMinLogRegion = 11;
 constexpr int kMaxLogRegion = 13;

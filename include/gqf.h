@@ -118,6 +118,24 @@ int gqf_bulk_delete_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t 
 int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* returns, uint8_t flags,
                        void* stream);
 
+/* No counterpart in the reference.  bulk_insert for callers that must not
+ * allocate device memory while they run (a process whose device budget is
+ * fixed at start-up, a plugin whose host framework owns all device memory, a
+ * loop that cannot take cudaMalloc's implicit synchronisation).  Same result
+ * as bulk_insert, on `stream` (NULL = legacy default stream); it calls no
+ * allocator.  The batch is partitioned into one fixed array of
+ * GQF_NOALLOC_SCRATCH_BYTES inside the library's device image, held by every
+ * GPU that loads the library: a batch may hold at most
+ *   (GQF_NOALLOC_SCRATCH_BYTES - 16 * (nslots / 2^region_log + 2), rounded up
+ *    to 256) / 4 keys
+ * (about 4.06 million at 2^28 slots); larger batches are refused with -1 and
+ * a message in gqf_last_error.  The first call on each device, with that
+ * device current, looks up the array's address: make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller.  Returns 0 on success. */
+#define GQF_NOALLOC_SCRATCH_BYTES (16u << 20)
+int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
+
 /* The filter's default stream for the reference entry points. */
 int gqf_set_stream(QF* qf, void* stream);
 
