@@ -66,6 +66,7 @@ SIGNATURES = {
     "gqf_device_bytes": (_u64, [_vp]),
     "gqf_get_status": (_int, [_vp, ctypes.POINTER(_u32)]),
     "gqf_clear_status": (_int, [_vp]),
+    "gqf_get_counters": (_int, [_vp, _vp, _int]),
     "gqf_reset": (_int, [_vp]),
     "gqf_export_size": (_u64, [_vp]),
     "gqf_export": (_int, [_vp, _vp, _u64]),
@@ -243,6 +244,11 @@ class QF:
         s = _u32(0)
         self._ok(self.L.gqf_get_status(self.h, ctypes.byref(s)))
         return int(s.value)
+
+    def counters(self) -> dict:
+        c = np.zeros(2, dtype=np.uint64)
+        self._ok(self.L.gqf_get_counters(self.h, c.ctypes.data, 2))
+        return {"deferred_regions": int(c[0]), "serial_keys": int(c[1])}
 
     def clear_status(self):
         self._ok(self.L.gqf_clear_status(self.h))

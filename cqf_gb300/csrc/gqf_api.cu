@@ -107,13 +107,14 @@ HostFilter* lookup(const QF* qf) {
 }
 
 int auto_log_region(int nbits) {
-  if (nbits >= 24) return 13;
-  if (nbits >= 21) return 12;
-  return 11;
+  // 2^12-quotient regions fit three rebuild CTAs per SM; small tables use
+  // 2^11 for more regions per phase.
+  return nbits >= 21 ? 12 : 11;
 }
 
 uint32_t* status_ptr(HostFilter* f) { return reinterpret_cast<uint32_t*>(f->aux); }
 unsigned long long* misses_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 64); }
+unsigned long long* stats_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 128); }
 
 uint32_t nregions_for(const HostFilter* f, int log_region) {
   uint64_t n = f->h.nslots >> log_region;
@@ -158,6 +159,7 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
   }
   f->part.nregions = nr;
   f->part.log_region = f->log_region;
+  f->part.stats = stats_ptr(f);
   return true;
 }
 
@@ -194,6 +196,7 @@ bool internal_view(const QF* qf, FilterView* v) {
   v->g = f->g;
   v->dqf = f->dqf;
   v->status = status_ptr(f);
+  v->stats = stats_ptr(f);
   v->log_region = f->log_region;
   v->nregions = nregions_for(f, f->log_region);
   v->stream = f->stream;
@@ -439,7 +442,19 @@ int gqf_get_status(QF* qf, uint32_t* status) {
 int gqf_clear_status(QF* qf) {
   HostFilter* f = lookup(qf);
   if (!f) return -1;
-  return ck(cudaMemsetAsync(status_ptr(f), 0, 4, f->stream), "memset status") ? 0 : -1;
+  return ck(cudaMemsetAsync(status_ptr(f), 0, 4, f->stream), "memset status") &&
+         ck(cudaMemsetAsync(stats_ptr(f), 0, 16, f->stream), "memset counters") ? 0 : -1;
+}
+
+int gqf_get_counters(QF* qf, uint64_t* counters, int n) {
+  HostFilter* f = lookup(qf);
+  if (!f || !counters || n < 0) return -1;
+  unsigned long long c[2] = {0, 0};
+  if (!ck(cudaMemcpyAsync(c, stats_ptr(f), 16, cudaMemcpyDeviceToHost, f->stream), "memcpy counters") ||
+      !ck(cudaStreamSynchronize(f->stream), "sync"))
+    return -1;
+  for (int i = 0; i < n && i < 2; i++) counters[i] = c[i];
+  return 0;
 }
 
 int gqf_reset(QF* qf) {

@@ -32,6 +32,7 @@ struct Partition {
   uint32_t* region_start;  // nregions + 1 (exclusive prefix)
   uint32_t* cursor;        // nregions
   uint32_t* deferred;      // [0] = n, then region ids
+  unsigned long long* stats;  // [0] regions deferred, [1] keys applied serially (or nullptr)
   uint32_t nregions;
   int log_region;          // a region is 2^log_region quotients
 };
@@ -43,6 +44,7 @@ struct FilterView {
   Geom g;
   quotient_filter* dqf;
   uint32_t* status;
+  unsigned long long* stats;
   int log_region;
   uint32_t nregions;
   cudaStream_t stream;

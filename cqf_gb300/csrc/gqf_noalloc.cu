@@ -94,6 +94,7 @@ extern "C" int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* k
   p.deferred = w + 3 * words;
   p.keys = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + table_bytes);
   p.counts = nullptr;
+  p.stats = v.stats;
   p.nregions = v.nregions;
   p.log_region = v.log_region;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

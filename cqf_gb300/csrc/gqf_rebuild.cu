@@ -12,10 +12,12 @@
 //     reference's schedule), so two CTAs never touch the same slots;
 //   * the CTA stages a window of LOGS-region + PUSH slots in shared memory
 //     (the region plus the head of the next one, which its growth may push);
-//   * it sorts the region's new keys in shared memory (bitonic), merges them
-//     run by run with the old counters (decode_counter / encode_counter,
-//     src/gqf.cu:1216-1345), and recomputes every run position with one
-//     block-wide max-plus scan: end(q) = max(q + L_q - 1, end(prev) + L_q);
+//   * it groups the region's new keys by quotient with a counting sort in
+//     shared memory, merges them with the old counters of the touched runs
+//     only (decode_counter / encode_counter, src/gqf.cu:1216-1345), and
+//     recomputes every run position with one block-wide max-plus scan:
+//     end(q) = max(q + L_q - 1, end(prev) + L_q);
+//   * untouched runs move byte-parallel (every slot knows its run's shift);
 //   * it writes back only the blocks that changed.
 //
 // A rebuild whose changes would reach past the window (a cluster longer than
@@ -33,36 +35,43 @@ constexpr int kNeg = -(1 << 28);  // "minus infinity" of the max-plus scan
 template <int LOGS>
 struct Cfg;
 template <>
-struct Cfg<11> { static constexpr int PUSH = 1024, NT = 256, KMAX = 2048; };
+struct Cfg<11> { static constexpr int PUSH = 1024, KMAX = 2048, MINB = 4; };
 template <>
-struct Cfg<12> { static constexpr int PUSH = 1024, NT = 256, KMAX = 4096; };
+struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 3; };
 template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, NT = 512, KMAX = 4096; };
+struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 1; };
 
 template <int LOGS>
 struct Lay {
+  static constexpr int NT = 256;
   static constexpr int REG = 1 << LOGS;
   static constexpr int PUSH = Cfg<LOGS>::PUSH;
-  static constexpr int NT = Cfg<LOGS>::NT;
   static constexpr int KMAX = Cfg<LOGS>::KMAX;
   static constexpr int WIN = REG + PUSH;
   static constexpr int WB = WIN / 64;
   static constexpr int QPT = WIN / NT;
-  static_assert(WIN % NT == 0, "quotients split evenly over threads");
+  static constexpr int KCW = REG / 2 + 2;  // packed 16-bit per-quotient key counters
+  static_assert(WIN % NT == 0 && (REG / 2) % NT == 0, "work splits evenly over threads");
   static_assert(PUSH < REG, "a window must not reach the region after next");
+  static_assert(WIN + PUSH + 64 < 32767, "window positions fit int16");
   // shared memory carve-up (bytes)
   static constexpr int IMG = WB * 96;
   static constexpr int OFF_IMG0 = 0;
   static constexpr int OFF_IMG1 = OFF_IMG0 + IMG;
-  static constexpr int OFF_KEYS = OFF_IMG1 + IMG;                 // u64[KMAX]
-  static constexpr int OFF_NOCC = OFF_KEYS + KMAX * 8;            // u64[WB]
-  static constexpr int OFF_TCH = OFF_NOCC + WB * 8;               // u64[WB]
-  static constexpr int OFF_RPOS = OFF_TCH + WB * 8;               // u16[WIN + 8]
-  static constexpr int OFF_PREF = OFF_RPOS + (WIN + 8) * 2;       // u16[WIN]
-  static constexpr int OFF_ORANK = OFF_PREF + WIN * 2;            // u16[WB + 1]
-  static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;      // u16[WB + 1]
+  static constexpr int OFF_KG = OFF_IMG1 + IMG;                  // u32[KMAX] keys grouped by quotient
+  static constexpr int OFF_KC = OFF_KG + KMAX * 4;               // u32[KCW]
+  static constexpr int OFF_RPOS = OFF_KC + KCW * 4;              // u16[WIN + 8] old run ends by rank
+  static constexpr int OFF_PREF = OFF_RPOS + (WIN + 8) * 2;      // u16[WIN] lengths, then ends + 1
+  static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8] old start, then shift
+  static constexpr int OFF_USED = OFF_DELTA + (WIN + 8) * 2;     // u32[WIN / 32] old run slots
+  static constexpr int OFF_NOCC = (OFF_USED + WIN / 8 + 7) & ~7; // u64[WB] new occupieds
+  static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
+  static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
+  static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;     // u16[WB + 8]
   static constexpr int BYTES = OFF_RRANK + (WB + 8) * 2;
 };
+
+constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
 
 // ----------------------------------------------------- shared-memory image
 
@@ -79,22 +88,21 @@ struct Img {
   }
 };
 
-// Merge one run's old counters with the run's sorted new keys and return the
-// new run length; with WRITE, also emit the bytes at out[pos..].
-//   keys[ki..kj): (local << 32) | multiplicity, sorted, all with this quotient.
+// Merge one run's old counters with the run's new keys (sorted by remainder,
+// one occurrence each) and return the new run length; with WRITE, also emit
+// the bytes at out[pos..].
 template <bool DEL, bool WRITE>
-__device__ int merge_run(Img cur, bool has_old, int s, int e, const unsigned long long* keys, int ki,
-                         int kj, Img out, int pos) {
+__device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* keys, int ki, int kj,
+                         Img out, int pos) {
   auto get = [&](uint64_t i) -> uint64_t { return cur.slot((int)i); };
   auto end = [&](uint64_t i) -> int { return cur.is_end((int)i); };
+  const uint64_t lim = (uint64_t)e + 1;  // the walk never leaves the run [s, e]
   int total = 0;
   bool have_old = has_old;
   int opos = s;
   uint32_t orem = 0;
   uint64_t ocnt = 0;
   int oend = 0;
-  // the walk never leaves the run [s, e]
-  const uint64_t lim = (uint64_t)e + 1;
   if (have_old) oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
   int j = ki;
   uint8_t enc[16];
@@ -103,42 +111,33 @@ __device__ int merge_run(Img cur, bool has_old, int s, int e, const unsigned lon
     uint64_t ncnt = 0;
     int jn = j;
     if (j < kj) {
-      nrem = (uint32_t)((keys[j] >> 32) & 255);
-      while (jn < kj && (uint32_t)((keys[jn] >> 32) & 255) == nrem) {
-        ncnt += keys[jn] & 0xFFFFFFFFULL;
+      nrem = keys[j] & 255u;
+      while (jn < kj && (keys[jn] & 255u) == nrem) {
+        ncnt++;
         jn++;
       }
     }
-    if (have_old && (j >= kj || orem < nrem)) {
+    bool take_old = have_old && (j >= kj || orem < nrem);
+    bool both = have_old && j < kj && orem == nrem;
+    if (take_old) {
       int len = oend - opos + 1;
       if (WRITE)
         for (int t = 0; t < len; t++) out.slot(pos + total + t) = cur.slot(opos + t);
       total += len;
-      if (cur.is_end(oend) || oend >= e) {
-        have_old = false;
-      } else {
-        opos = oend + 1;
-        oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
-      }
     } else {
-      uint64_t c;
-      bool advance_old = have_old && orem == nrem;
-      if (advance_old)
-        c = DEL ? (ocnt > ncnt ? ocnt - ncnt : 0) : ocnt + ncnt;
-      else
-        c = DEL ? 0 : ncnt;
+      uint64_t c = both ? (DEL ? (ocnt > ncnt ? ocnt - ncnt : 0) : ocnt + ncnt) : (DEL ? 0 : ncnt);
       int len = encode_counter(nrem, c, enc);
       if (WRITE)
         for (int t = 0; t < len; t++) out.slot(pos + total + t) = enc[t];
       total += len;
       j = jn;
-      if (advance_old) {
-        if (cur.is_end(oend) || oend >= e) {
-          have_old = false;
-        } else {
-          opos = oend + 1;
-          oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
-        }
+    }
+    if (take_old || both) {
+      if (cur.is_end(oend) || oend >= e) {
+        have_old = false;
+      } else {
+        opos = oend + 1;
+        oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
       }
     }
   }
@@ -171,10 +170,9 @@ __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
     sb[lane] = wb;
   }
   __syncthreads();
-  // exclusive within warp
   int ea = __shfl_up_sync(0xffffffffu, ia, 1), eb = __shfl_up_sync(0xffffffffu, ib, 1);
   if (lane == 0) { ea = kNeg; eb = 0; }
-  if (wid > 0) {  // prefix of earlier warps first
+  if (wid > 0) {
     int pa = sa[wid - 1], pb = sb[wid - 1];
     ea = max(ea, pa + eb);
     eb = pb + eb;
@@ -184,11 +182,37 @@ __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
   __syncthreads();
 }
 
+// Block-wide exclusive sum; returns this thread's prefix and the total.
+template <int NT>
+__device__ int scan_sum(int v, int* tmp, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) tmp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < NT / 32 ? tmp[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    tmp[lane] = w;
+  }
+  __syncthreads();
+  int r = x - v + (wid ? tmp[wid - 1] : 0);
+  *total = tmp[NT / 32 - 1];
+  __syncthreads();
+  return r;
+}
+
 template <int LOGS, bool DEL>
-__global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition p, int parity,
-                                                            uint32_t* status) {
+__global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partition p, int parity,
+                                                                   uint32_t* status) {
   using L = Lay<LOGS>;
-  constexpr int NT = L::NT, WB = L::WB, QPT = L::QPT, KMAX = L::KMAX;
+  constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
   extern __shared__ __align__(128) uint8_t sm[];
   __shared__ int s_i[8];
   __shared__ int sa[32], sb[32];
@@ -197,20 +221,25 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
   if (r >= p.nregions) return;
   const uint32_t kbeg = p.region_start[r], kend = p.region_start[r + 1];
   if (kbeg == kend) return;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
   const uint64_t base = (uint64_t)r << LOGS;
   const uint64_t bw0 = base >> 6;
   const int wb = (int)min((uint64_t)WB, g.nblocks - bw0);
-  const int win_valid = (int)min((uint64_t)wb * 64, g.xnslots - base);
-  const int win_q = (int)min((uint64_t)L::WIN, g.nslots - base);
+  const int wslots = wb * 64;
+  const int win_valid = (int)min((uint64_t)wslots, g.xnslots - base);
+  const int win_q = (int)min((uint64_t)WIN, g.nslots - base);
   const int wq_words = (win_q + 63) >> 6;
+  const int nq = (int)min((uint64_t)REG, g.nslots - base);
 
-  unsigned long long* keys = reinterpret_cast<unsigned long long*>(sm + L::OFF_KEYS);
-  unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
-  unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
+  uint32_t* kg = reinterpret_cast<uint32_t*>(sm + L::OFF_KG);
+  uint32_t* kc = reinterpret_cast<uint32_t*>(sm + L::OFF_KC);
   uint16_t* rpos = reinterpret_cast<uint16_t*>(sm + L::OFF_RPOS);
   uint16_t* pref = reinterpret_cast<uint16_t*>(sm + L::OFF_PREF);
+  int16_t* delta = reinterpret_cast<int16_t*>(sm + L::OFF_DELTA);
+  uint32_t* used = reinterpret_cast<uint32_t*>(sm + L::OFF_USED);
+  unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
+  unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
   uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
   uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
 
@@ -222,56 +251,72 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
   }
   __syncthreads();
   const int c0 = (int)Img{sm + L::OFF_IMG0}.off(0) - 1;  // last slot used by earlier regions' runs
-  int cur = 0;
-  int dirty_lo = 1 << 30, dirty_hi = -1;
   // The previous region's runs fill the whole window: every run of this
   // region lies beyond it, so only the serial path can place them.  (This
   // also keeps all window positions far below the 16-bit tables' range.)
   bool deferred = c0 + 1 >= win_valid;
+  const bool multi = kend - kbeg > (uint32_t)KMAX;
+  int cur = 0;
+  bool changed = false;
+
+  auto kcnt = [&](int q) -> int { return (int)((kc[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu); };
+  // runends of word w that lie after c0
+  auto runs_after_c0 = [&](Img C, int w) -> unsigned long long {
+    unsigned long long rw = C.run(w);
+    int lo = 64 * w;
+    if (c0 >= lo + 63) return 0ULL;
+    if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
+    return rw;
+  };
 
   for (uint32_t kr = kbeg; kr < kend && !deferred; kr += KMAX) {
     const int nk = (int)min((uint32_t)KMAX, kend - kr);
-    int P = 2;
-    while (P < nk) P <<= 1;
-    for (int i = tid; i < P; i += NT)
-      keys[i] = i < nk ? (((unsigned long long)p.keys[kr + i]) << 32) |
-                             (p.counts ? (unsigned long long)p.counts[kr + i] : 1ULL)
-                       : ~0ULL;
-    for (int i = tid; i < WB; i += NT) { nocc[i] = 0; tch[i] = 0; }
-    __syncthreads();
-    // bitonic sort of the round's keys
-    for (int k = 2; k <= P; k <<= 1) {
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = tid; i < P; i += NT) {
-          int ixj = i ^ j;
-          if (ixj > i) {
-            unsigned long long a = keys[i], b = keys[ixj];
-            bool up = (i & k) == 0;
-            if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
-          }
-        }
-        __syncthreads();
-      }
-    }
-
     const Img C{sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0)};
     const Img N{sm + (cur ? L::OFF_IMG0 : L::OFF_IMG1)};
 
-    // ---- rank tables: occupied quotients per word, runends after c0 per word
-    if (tid < 32) {
-      const int lane = tid;
-      int per = (WB + 31) / 32;
+    // ---- group this round's keys by quotient (counting sort in shared memory)
+    for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
+    for (int i = tid; i < WB; i += NT) { nocc[i] = 0; tch[i] = 0; }
+    for (int i = tid; i < WIN / 32; i += NT) used[i] = 0;
+    __syncthreads();
+    for (int i = tid; i < nk; i += NT) {
+      uint32_t q = p.keys[kr + i] >> 8;
+      atomicAdd(&kc[q >> 1], 1u << ((q & 1) * 16));
+    }
+    __syncthreads();
+    {  // exclusive prefix over the REG counters, 2 per word
+      constexpr int WPT = (REG / 2) / NT;
+      int a = tid * WPT, sum = 0;
+      for (int w = a; w < a + WPT; w++) sum += (int)(kc[w] & 0xFFFFu) + (int)(kc[w] >> 16);
+      int tot;
+      int run = scan_sum<NT>(sum, sa, &tot);
+      for (int w = a; w < a + WPT; w++) {
+        uint32_t v = kc[w];
+        uint32_t lo = (uint32_t)run;
+        run += (int)(v & 0xFFFFu);
+        uint32_t hi = (uint32_t)run;
+        run += (int)(v >> 16);
+        kc[w] = lo | (hi << 16);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < nk; i += NT) {
+      uint32_t key = p.keys[kr + i];
+      uint32_t q = key >> 8;
+      uint32_t sh = (q & 1) * 16;
+      uint32_t old = atomicAdd(&kc[q >> 1], 1u << sh);
+      kg[(old >> sh) & 0xFFFFu] = key;
+    }
+    // now the keys of quotient q are kg[q ? kcnt(q-1) : 0, kcnt(q))
+
+    // ---- rank tables of the current image
+    if (wid == 0) {
+      constexpr int per = (WB + 31) / 32;
       int a = lane * per, b = min(a + per, WB);
       int so = 0, sr = 0;
       for (int w = a; w < b; w++) {
         if (w < wq_words) so += __popcll(C.occ(w));
-        if (w < wb) {
-          unsigned long long rw = C.run(w);
-          int lo = 64 * w;
-          if (c0 >= lo + 63) rw = 0;
-          else if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
-          sr += __popcll(rw);
-        }
+        if (w < wb) sr += __popcll(runs_after_c0(C, w));
       }
       int io = so, ir = sr;
       for (int o = 1; o < 32; o <<= 1) {
@@ -283,29 +328,16 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
         orank[w] = (uint16_t)eo;
         rrank[w] = (uint16_t)er;
         if (w < wq_words) eo += __popcll(C.occ(w));
-        if (w < wb) {
-          unsigned long long rw = C.run(w);
-          int lo = 64 * w;
-          if (c0 >= lo + 63) rw = 0;
-          else if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
-          er += __popcll(rw);
-        }
+        if (w < wb) er += __popcll(runs_after_c0(C, w));
       }
-      if (lane == 31) { s_i[0] = ir; }  // visible runends after c0
+      if (lane == 31) { s_i[0] = ir; s_i[1] = io; }  // visible runends, occupied quotients
     }
     __syncthreads();
-    const int nvis = s_i[0];
-    for (int w = tid; w < wb; w += NT) {
-      unsigned long long rw = C.run(w);
-      int lo = 64 * w;
-      if (c0 >= lo + 63) rw = 0;
-      else if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
-      int k = rrank[w];
-      while (rw) {
-        int bit = __ffsll((long long)rw) - 1;
-        rpos[k++] = (uint16_t)(lo + bit);
-        rw &= rw - 1;
-      }
+    const int nvis = s_i[0], nold = s_i[1];
+    for (int sl = tid; sl < wslots; sl += NT) {
+      unsigned long long rw = runs_after_c0(C, sl >> 6);
+      if ((rw >> (sl & 63)) & 1ULL)
+        rpos[rrank[sl >> 6] + __popcll(rw & ((1ULL << (sl & 63)) - 1ULL))] = (uint16_t)sl;
     }
     __syncthreads();
 
@@ -314,56 +346,72 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
     auto rank_of = [&](int q) -> int {
       return (int)orank[q >> 6] + __popcll(C.occ(q >> 6) & ((1ULL << (q & 63)) - 1ULL));
     };
-    auto old_run = [&](int q, int& s, int& e) {
-      int k = rank_of(q);
-      e = runpos(k);
-      int pe = k ? runpos(k - 1) : c0;
-      s = max(q, pe + 1);
-    };
 
-    // ---- per-quotient new run lengths; compose this thread's max-plus map
-    const int qa = tid * QPT, qb = min(qa + QPT, win_q);
-    int lo_k = 0, hi_k = nk;  // first key with quotient >= qa
-    {
-      unsigned long long probe = ((unsigned long long)qa) << 40;
-      while (lo_k < hi_k) {
-        int mid = (lo_k + hi_k) >> 1;
-        if (keys[mid] < probe) lo_k = mid + 1; else hi_k = mid;
+    // ---- pass A: old run of every quotient (uniform across lanes)
+    for (int q = tid; q < win_q; q += NT) {
+      int len = 0;
+      if ((C.occ(q >> 6) >> (q & 63)) & 1ULL) {
+        const int k = rank_of(q);
+        const int e = runpos(k);
+        const int s = max(q, (k ? runpos(k - 1) : c0) + 1);
+        len = e - s + 1;
+        delta[k] = (int16_t)s;
+        const int last = min(e, wslots - 1);
+        for (int x = s; x <= last;) {  // mark the run's slots
+          const int hi = min(last, x | 31);
+          const int hb = hi & 31;
+          atomicOr(&used[x >> 5], (hb == 31 ? ~0u : ((2u << hb) - 1u)) & (~0u << (x & 31)));
+          x = hi + 1;
+        }
       }
+      pref[q] = (uint16_t)len;
     }
-    int fa = kNeg, fb = 0;
+    __syncthreads();
+    // ---- merge tasks: one per touched quotient (the first key of each group)
     bool my_defer = false;
-    {
-      int ki = lo_k;
-      for (int q = qa; q < qb; q++) {
-        const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
-        int kj = ki;
-        while (kj < nk && (int)(keys[kj] >> 40) == q) kj++;
-        int s = 0, e = -1, len = 0;
-        if (occ) { old_run(q, s, e); len = e - s + 1; }
-        if (kj > ki) {
-          atomicOr(&tch[q >> 6], 1ULL << (q & 63));
-          if (occ && e >= win_valid) {
-            my_defer = true;
-          } else {
-            len = merge_run<DEL, false>(C, occ, s, e, keys, ki, kj, N, 0);
-          }
-        }
-        pref[q] = (uint16_t)len;
-        if (len > 0) {
-          atomicOr(&nocc[q >> 6], 1ULL << (q & 63));
-          // compose f_q after the running map: f_q(x) = max(q + len - 1, x + len)
-          fa = max(q + len - 1, fa + len);
-          fb = fb + len;
-        }
-        ki = kj;
+    for (int i = tid; i < nk; i += NT) {
+      const uint32_t q = kg[i] >> 8;
+      if (i > 0 && (kg[i - 1] >> 8) == q) continue;
+      const int ks = i, ke = kcnt((int)q);
+      atomicOr(&tch[q >> 6], 1ULL << (q & 63));
+      const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
+      int s = 0, e = -1;
+      if (occ) {
+        const int k = rank_of((int)q);
+        e = runpos(k);
+        s = delta[k];
       }
+      if (occ && e >= win_valid) {
+        my_defer = true;
+        continue;
+      }
+      for (int a = ks + 1; a < ke; a++) {  // the quotient's keys by remainder
+        const uint32_t v = kg[a];
+        int b = a;
+        while (b > ks && kg[b - 1] > v) { kg[b] = kg[b - 1]; b--; }
+        kg[b] = v;
+      }
+      pref[q] = (uint16_t)merge_run<DEL, false>(C, occ, s, e, kg, ks, ke, N, 0);
     }
     if (__syncthreads_or(my_defer)) { deferred = true; break; }
+    // ---- new occupancy: 32 quotients per warp ballot
+    for (int q0 = 0; q0 < WIN; q0 += NT) {
+      const int q = q0 + tid;
+      const unsigned bal = __ballot_sync(0xffffffffu, q < win_q && pref[q] > 0);
+      const int qw = q0 + wid * 32;
+      if (lane == 0 && bal) atomicOr(reinterpret_cast<uint32_t*>(&nocc[qw >> 6]) + ((qw >> 5) & 1), bal);
+    }
+    __syncthreads();
 
-    // ---- block scan: where does each thread's first quotient start from?
-    scan_maps<NT>(fa, fb, sa, sb);
+    // ---- run positions: one block-wide max-plus scan over the quotients
     {
+      const int qa = tid * QPT, qb = min(qa + QPT, win_q);
+      int fa = kNeg, fb = 0;
+      for (int q = qa; q < qb; q++) {
+        int len = pref[q];
+        if (len > 0) { fa = max(q + len - 1, fa + len); fb += len; }
+      }
+      scan_maps<NT>(fa, fb, sa, sb);
       int x = max(fa, c0 + fb);  // end of all runs before qa
       for (int q = qa; q < qb; q++) {
         int len = pref[q];
@@ -372,106 +420,79 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
       }
     }
     __syncthreads();
-
-    // ---- what changed?
-    int qlo = 1 << 30, hi = -1;
-    for (int q = qa; q < qb; q++) {
-      const bool oo = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
-      const bool no = (nocc[q >> 6] >> (q & 63)) & 1ULL;
-      if (!oo && !no) continue;
-      const bool touched = (tch[q >> 6] >> (q & 63)) & 1ULL;
-      int s = 0, e = -1;
-      if (oo) old_run(q, s, e);
-      int ne = (int)pref[q] - 1;
-      int prev = q ? (int)pref[q - 1] - 1 : c0;
-      int ns = max(q, prev + 1);
-      bool changed = touched || oo != no || (no && (ns != s || ne != e));
-      if (changed) {
-        qlo = min(qlo, q);
-        if (oo) hi = max(hi, e);
-        if (no) hi = max(hi, ne);
-      }
-    }
-    // block min / max
-    for (int o = 16; o; o >>= 1) {
-      qlo = min(qlo, __shfl_xor_sync(0xffffffffu, qlo, o));
-      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    if (tid == 0) { s_i[1] = 1 << 30; s_i[2] = -1; }
-    __syncthreads();
-    if ((tid & 31) == 0) { atomicMin(&s_i[1], qlo); atomicMax(&s_i[2], hi); }
-    __syncthreads();
-    qlo = s_i[1];
-    hi = s_i[2];
-    if (hi < 0) continue;  // nothing changed in this round
-    if (hi >= win_valid) { deferred = true; break; }
-    // first slot that may change: start of the first changed run (old or new)
-    int lo_slot;
     {
-      int prev = qlo ? (int)pref[qlo - 1] - 1 : c0;
-      int ns = max(qlo, prev + 1);
-      lo_slot = ns;
-      if ((C.occ(qlo >> 6) >> (qlo & 63)) & 1ULL) {
-        int s, e;
-        old_run(qlo, s, e);
-        lo_slot = min(lo_slot, s);
-      }
+      const int e_old = nold ? runpos(nold - 1) : c0;
+      const int e_new = (int)pref[win_q - 1] - 1;
+      // A change that reaches the window's end would move runs this CTA does
+      // not hold (or overflow the table): leave the region to the serial pass.
+      if (e_new != e_old && max(e_new, e_old) >= win_valid) { deferred = true; break; }
     }
 
-    // ---- build the next image: copy, clear [lo_slot, hi], write runs
+    // ---- build the next image: clear, keep the previous region's spill
     {
-      const uint4* src = reinterpret_cast<const uint4*>(C.p);
       uint4* dst = reinterpret_cast<uint4*>(N.p);
-      for (int i = tid; i < wb * 6; i += NT) dst[i] = src[i];
+      for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
-    for (int i = lo_slot + tid; i <= hi; i += NT) N.slot(i) = 0;
-    for (int w = (lo_slot >> 6) + tid; w <= (hi >> 6); w += NT) {
-      int a = max(lo_slot, 64 * w) - 64 * w, b = min(hi, 64 * w + 63) - 64 * w;  // inclusive bit range
-      unsigned long long m = (b == 63 ? ~0ULL : ((1ULL << (b + 1)) - 1ULL)) & (~0ULL << a);
-      N.run(w) &= ~m;
+    for (int sl = tid; sl <= c0 && sl < wslots; sl += NT) N.slot(sl) = C.slot(sl);
+    for (int w = tid; w < wb && 64 * w <= c0; w += NT) {
+      int nb = c0 - 64 * w;  // bits 0..nb belong to the previous region's runs
+      N.run(w) = nb >= 63 ? C.run(w) : (C.run(w) & ((2ULL << nb) - 1ULL));
     }
     __syncthreads();
-    for (int q = max(qa, qlo); q < qb; q++) {
-      if (!((nocc[q >> 6] >> (q & 63)) & 1ULL)) continue;
-      int ne = (int)pref[q] - 1;
-      int prev = q ? (int)pref[q - 1] - 1 : c0;
-      int ns = max(q, prev + 1);
-      if (ns > hi) break;
-      if ((tch[q >> 6] >> (q & 63)) & 1ULL) {
-        int kj, ki;
-        {  // keys of q
-          unsigned long long probe = ((unsigned long long)q) << 40;
-          int l = 0, h = nk;
-          while (l < h) { int m = (l + h) >> 1; if (keys[m] < probe) l = m + 1; else h = m; }
-          ki = l;
-          kj = ki;
-          while (kj < nk && (int)(keys[kj] >> 40) == q) kj++;
-        }
-        const bool oo = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
-        int s = 0, e = -1;
-        if (oo) old_run(q, s, e);
-        merge_run<DEL, true>(C, oo, s, e, keys, ki, kj, N, ns);
-      } else {
-        int s, e;
-        old_run(q, s, e);
-        if (e >= win_valid || ne >= win_valid) continue;  // cannot happen: checked above
-        for (int t = 0; t <= e - s; t++) N.slot(ns + t) = C.slot(s + t);
+    // ---- pass B: shift of every untouched run, runends of the new layout
+    for (int q = tid; q < win_q; q += NT) {
+      const bool no = (nocc[q >> 6] >> (q & 63)) & 1ULL;
+      const int ne = (int)pref[q] - 1;
+      if (no && ne < wslots) N.set_end(ne);
+      if ((C.occ(q >> 6) >> (q & 63)) & 1ULL) {
+        const bool touched = q < nq && ((tch[q >> 6] >> (q & 63)) & 1ULL);
+        const int k = rank_of(q);
+        const int ns = max(q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
+        delta[k] = touched ? kTouched : (int16_t)(ns - delta[k]);
       }
-      N.set_end(ne);
     }
-    // occupieds of the window's quotient words
-    for (int w = tid; w < wq_words; w += NT) N.occ(w) = nocc[w];
-    // offsets of blocks 1 .. hi/64 (block 0 belongs to the previous region)
-    for (int w = 1 + tid; w <= min(wb - 1, hi >> 6); w += NT) {
-      int x = min(64 * w - 1, win_q - 1);
-      int E = (int)pref[x] - 1;
-      if (E < win_valid) N.off(w) = (uint32_t)max(0, E - 64 * w + 1);
+    // ---- merge tasks again, now writing the touched runs at their new start
+    for (int i = tid; i < nk; i += NT) {
+      const uint32_t q = kg[i] >> 8;
+      if (i > 0 && (kg[i - 1] >> 8) == q) continue;
+      if (!((nocc[q >> 6] >> (q & 63)) & 1ULL)) continue;  // deleted entirely
+      const int ks = i, ke = kcnt((int)q);
+      const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
+      int s = 0, e = -1;
+      if (occ) {
+        const int k = rank_of((int)q);
+        e = runpos(k);
+        s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
+      }
+      const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
+      merge_run<DEL, true>(C, occ, s, e, kg, ks, ke, N, ns);
     }
     __syncthreads();
-    dirty_lo = min(dirty_lo, min(qlo, lo_slot) >> 6);
-    dirty_hi = max(dirty_hi, hi >> 6);
+    // ---- slot pass: every untouched run's bytes move by their run's shift
+    for (int sl = tid; sl < wslots; sl += NT) {
+      if (!((used[sl >> 5] >> (sl & 31)) & 1u)) continue;
+      const int w = sl >> 6;
+      const int k = rrank[w] + __popcll(runs_after_c0(C, w) & ((1ULL << (sl & 63)) - 1ULL));
+      const int d = delta[k];
+      if (d == kTouched) continue;
+      const int t = sl + d;
+      if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
+    }
+    // ---- block headers: occupieds and offsets
+    for (int w = tid; w < wb; w += NT) {
+      N.occ(w) = w < wq_words ? nocc[w] : 0ULL;
+      if (w == 0) {
+        N.off(0) = C.off(0);
+      } else {
+        const int x = min(64 * w - 1, win_q - 1);
+        const int E = (int)pref[x] - 1;
+        N.off(w) = E >= win_valid ? C.off(w) : (uint32_t)max(0, E - 64 * w + 1);
+      }
+    }
+    __syncthreads();
     cur ^= 1;
+    changed = true;
   }
 
   if (deferred) {
@@ -479,15 +500,26 @@ __global__ void __launch_bounds__(Lay<LOGS>::NT, 1) k_rebuild(Geom g, Partition 
       uint32_t at = atomicAdd(&p.deferred[0], 1u);
       p.deferred[1 + at] = r;
       atomicOr(status, kStDeferred);
+      if (p.stats) atomicAdd(&p.stats[0], 1ULL);
     }
     return;
   }
-  if (dirty_hi < 0) return;
+  if (!changed) return;
+  // ---- write back the blocks that differ from what was loaded
   {
-    const uint4* src = reinterpret_cast<const uint4*>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0)) + dirty_lo * 6;
-    uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0 + dirty_lo);
-    const int n16 = (dirty_hi - dirty_lo + 1) * 6;
-    for (int i = tid; i < n16; i += NT) dst[i] = src[i];
+    const uint4* fin = reinterpret_cast<const uint4*>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
+    const uint4* org = reinterpret_cast<const uint4*>(sm + L::OFF_IMG0);
+    uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0);
+    for (int w = tid; w < wb; w += NT) {
+      bool diff = multi;  // after several rounds the loaded image is gone
+      if (!diff)
+        for (int c = 0; c < 6; c++) {
+          uint4 a = fin[w * 6 + c], b = org[w * 6 + c];
+          diff |= (a.x != b.x) | (a.y != b.y) | (a.z != b.z) | (a.w != b.w);
+        }
+      if (diff)
+        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
+    }
   }
 }
 
@@ -509,6 +541,7 @@ __global__ void k_fallback(quotient_filter* dqf, Partition p, int del, uint32_t*
   const int shift = 8 + p.log_region;
   for (uint32_t i = 0; i < n; i++) {
     uint32_t r = ids[i];
+    if (p.stats) p.stats[1] += p.region_start[r + 1] - p.region_start[r];
     for (uint32_t k = p.region_start[r]; k < p.region_start[r + 1]; k++) {
       uint64_t h = ((uint64_t)r << shift) | p.keys[k];
       uint64_t c = p.counts ? p.counts[k] : 1;
@@ -529,6 +562,8 @@ cudaError_t run_phases(const Geom& g, const Partition& p, Op op, uint32_t* statu
   if (!configured) {
     cudaFuncSetAttribute(k_rebuild<LOGS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
     cudaFuncSetAttribute(k_rebuild<LOGS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
+    cudaFuncSetAttribute(k_rebuild<LOGS, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_rebuild<LOGS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     configured = true;
   }
   const uint32_t half = (p.nregions + 1) / 2;

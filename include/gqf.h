@@ -157,6 +157,11 @@ uint64_t gqf_device_bytes(QF* qf);
 int gqf_get_status(QF* qf, uint32_t* status);
 int gqf_clear_status(QF* qf);
 
+/* Counters since the last gqf_clear_status: [0] regions whose rebuild window
+ * was exceeded (applied by the serial path), [1] keys applied serially.
+ * Writes min(n, 2) values; synchronises the filter's stream. */
+int gqf_get_counters(QF* qf, uint64_t* counters, int n);
+
 /* Empty the filter (asynchronous). */
 int gqf_reset(QF* qf);
 

@@ -153,12 +153,12 @@ def _one_per_quotient(q_lo, q_hi, seed):
 
 @pytest.mark.parametrize("lr", [11, 12])
 def test_long_cluster_defers_and_matches_oracle(gq, lr):
-    """A push that is not absorbed inside the rebuild window (here ~1600
-    slots with no gap) takes the serial path; the result is still the
-    reference's layout, byte for byte."""
+    """A push that is not absorbed inside the rebuild window (here ~2900
+    slots with no gap, longer than any push window) takes the serial path;
+    the result is still the reference's layout, byte for byte."""
     nbits = 14
     reg = 1 << lr
-    fill = _one_per_quotient(reg - 300, reg + 1300, 1)  # one key per slot, no gaps
+    fill = _one_per_quotient(reg - 300, reg + 2600, 1)  # one key per slot, no gaps
     extra = _clustered_hashes(2, nbits, 100, reg - 300, reg - 250)
     o = oracle.Oracle(nbits)
     with gq.QF(nbits, log_region=lr) as qf:
