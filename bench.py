@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--get-log", type=int, default=26)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
     return ap.parse_args()
 
@@ -324,6 +325,11 @@ def run_gpu(args, wl, rank, world):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = run_cpu_sample(wl, keys, absent, args)
 
+    ref_cuda = None
+    if rank == 0 and world == 1 and not args.no_ref_cuda:
+        qf.close()
+        ref_cuda = run_ref_cuda(wl, keys, absent, ops, value, torch)
+
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -345,6 +351,7 @@ def run_gpu(args, wl, rank, world):
         "roofline": roofline,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "ref_cuda": ref_cuda,
         "clocks": clk,
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches // args.steps),
@@ -426,6 +433,68 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch):
         "d2h_bytes_per_step": 8 * 2 * wl.n_get,
         "path": "C ABI (gqf_bulk_*_async) from pinned host buffers, copies on a second stream",
         "present_all_found": found,
+    }
+
+
+def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
+    """The reference's own CUDA build (its kernels compiled from its sources,
+    driven by oracle/refgpu.py) on the same step, timed per call by wall
+    clock around a synchronised call (the reference synchronises inside each
+    bulk call).  Keys are copied to a scratch buffer before each call, outside
+    the timing, because the reference overwrites them."""
+    from oracle import refgpu
+
+    if not refgpu.available():
+        return {"unavailable": "reference cubin not built (needs the reference tree on an x86 host)"}
+    r = refgpu.RefGPU(wl.nbits)
+    scratch = torch.empty(wl.batch, dtype=torch.int64, device="cuda")
+    out = torch.empty(wl.n_get, dtype=torch.int64, device="cuda")
+    t = {"insert": 0.0, "get": 0.0, "delete": 0.0}
+    try:
+        for s0, n in wl.batches:
+            scratch[:n].copy_(keys[s0:s0 + n])
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            r.bulk_insert(scratch, n)
+            torch.cuda.synchronize()
+            t["insert"] += time.perf_counter() - a
+        for probe in (keys[: wl.n_get], absent):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            r.bulk_get(probe, out)
+            torch.cuda.synchronize()
+            t["get"] += time.perf_counter() - a
+        r.bulk_get(keys[: wl.n_get], out)
+        torch.cuda.synchronize()
+        found = bool((out > 0).all().item())
+        for s0 in range(0, wl.n_get, wl.batch):
+            n = min(wl.batch, wl.n_get - s0)
+            scratch[:n].copy_(keys[s0:s0 + n])
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            r.bulk_delete(scratch, n)
+            torch.cuda.synchronize()
+            t["delete"] += time.perf_counter() - a
+    finally:
+        r.close()
+    total = sum(t.values())
+    rates = {"insert_mkeys_s": wl.n_insert / t["insert"] / 1e6,
+             "get_mkeys_s": 2 * wl.n_get / t["get"] / 1e6,
+             "delete_mkeys_s": wl.n_get / t["delete"] / 1e6}
+    return {
+        "value": round(wl.key_ops / total / 1e6, 3),
+        "unit": UNIT,
+        "seconds": round(total, 3),
+        "ops": {k: round(v, 3) for k, v in rates.items()},
+        "speedup": {
+            "step": round(ours_value / (wl.key_ops / total / 1e6), 2),
+            "insert": round(ours_ops["insert"]["mkeys_s"] / rates["insert_mkeys_s"], 2),
+            "get": round(ours_ops["get"]["mkeys_s"] / rates["get_mkeys_s"], 2),
+            "delete": round(ours_ops["delete"]["mkeys_s"] / rates["delete_mkeys_s"], 2),
+        },
+        "present_all_found": found,
+        "what": "reference src/gqf.cu kernels compiled for sm_103a from its sources; host orchestration "
+                "restated (oracle/refgpu.py), thrust::sort replaced by torch.sort",
     }
 
 

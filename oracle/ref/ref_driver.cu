@@ -11,6 +11,7 @@
 // regions (src/gqf.cu:2646-2750), and each region's keys are applied in order
 // with qf_insert / qf_remove under QF_NO_LOCK | QF_KEY_IS_HASH
 // (src/gqf.cu:2759-2906), even regions first, then odd ones.
+#include <stddef.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -162,6 +163,23 @@ int ref_insert_not_exists_hash(void* p, uint64_t hash, uint8_t* retval) {
 uint64_t ref_query_hash(void* p, uint64_t hash) {
   uint64_t v = 0;
   return qf_query((QF*)p, hash, &v, QF_NO_LOCK | QF_KEY_IS_HASH);
+}
+
+// Byte layout of the reference's device-visible structs as its compiler laid
+// them out: what a driver-API launcher must build in device memory.
+void ref_layout(uint64_t* out) {
+  out[0] = sizeof(QF);
+  out[1] = offsetof(QF, runtimedata);
+  out[2] = offsetof(QF, metadata);
+  out[3] = offsetof(QF, blocks);
+  out[4] = sizeof(qfruntime);
+  out[5] = offsetof(qfruntime, num_locks);
+  out[6] = offsetof(qfruntime, locks);
+  out[7] = offsetof(qfruntime, buffers);
+  out[8] = offsetof(qfruntime, buffer_sizes);
+  out[9] = sizeof(qfmetadata);
+  out[10] = sizeof(qfblock);
+  out[11] = offsetof(qfruntime, wait_times);
 }
 
 }  // extern "C"
