@@ -180,13 +180,18 @@ def measured_peak():
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the rebuild and probe kernels from the
-    committed ncu summary (profiles/ncu_traffic.json), if present."""
+    """DRAM bytes per unit of work (probe, key or block) of each kernel from
+    the committed ncu summaries (profiles/ncu_traffic.txt)."""
+    out = {}
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
-            return json.load(fh)
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.txt")) as fh:
+            for ln in fh:
+                p = ln.split()
+                if len(p) >= 3 and not ln.startswith("#"):
+                    out[p[0]] = (float(p[1]), p[2])
     except Exception:
-        return {}
+        pass
+    return out
 
 
 # --------------------------------------------------------------- GPU arm
@@ -304,7 +309,17 @@ def run_gpu(args, wl, rank, world):
         }
     dom = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
     d = kernels[dom]
-    traffic = profile_traffic().get(dom)
+    units_per_launch = {
+        "probe_get": wl.n_get,
+        "rebuild_insert": wl.n_insert / max(1, 2 * len(wl.batches)),
+        "rebuild_delete": wl.n_get / max(1, 2 * ((wl.n_get + wl.batch - 1) // wl.batch)),
+        "partition": (wl.n_insert + wl.n_get) / max(1, kernels.get("partition", {}).get("calls_per_step", 1)),
+    }
+    tr = profile_traffic()
+    for k, kd in kernels.items():
+        if k in tr:
+            kd["dram_bytes_per_launch"] = tr[k][0] * units_per_launch[k]
+    traffic = {"bytes_per_launch": kernels[dom]["dram_bytes_per_launch"]} if "dram_bytes_per_launch" in kernels[dom] else None
     roofline = {
         "bound": "hbm",
         "kernel": dom,

@@ -18,12 +18,17 @@ namespace {
 
 __device__ __forceinline__ uint64_t ld_u64(const unsigned long long* p) { return __ldg(p); }
 
-// Walks one run from `start`; returns the count for `rem` or 0.
+// Walks one run from `start`; returns the count for `rem` or 0.  The slots
+// come through a 16-byte register window and the runends through a one-word
+// register cache seeded with the home block's word, so a probe costs one
+// header load and usually one slot load, whatever the L1 hit rate.
 __device__ __forceinline__ uint64_t scan_run(const Block* __restrict__ B, uint64_t nblocks,
-                                             uint64_t start, uint32_t rem) {
-  // one-block cache of the runends word; slot bytes come through L1
-  uint64_t cb = start >> 6;
-  uint64_t cw = cb < nblocks ? ld_u64(&B[cb].runends) : 0;
+                                             uint64_t start, uint32_t rem, uint64_t home,
+                                             uint64_t home_runends) {
+  uint64_t cb = home;
+  uint64_t cw = home_runends;
+  uint64_t ci = ~0ULL;  // 16-slot chunk index held in `chunk`
+  uint4 chunk = make_uint4(0, 0, 0, 0);
   auto is_end = [&](uint64_t i) -> int {
     uint64_t bi = i >> 6;
     if (bi != cb) {
@@ -33,8 +38,16 @@ __device__ __forceinline__ uint64_t scan_run(const Block* __restrict__ B, uint64
     return (int)((cw >> (i & 63)) & 1ULL);
   };
   auto get = [&](uint64_t i) -> uint64_t {
-    uint64_t bi = i >> 6;
-    return bi < nblocks ? (uint64_t)__ldg(&B[bi].slots[i & 63]) : 0;
+    uint64_t c = i >> 4;
+    if (c != ci) {
+      ci = c;
+      uint64_t bi = i >> 6;
+      chunk = bi < nblocks ? __ldg(reinterpret_cast<const uint4*>(&B[bi].slots[(i & 63) & ~15ULL]))
+                           : make_uint4(0, 0, 0, 0);
+    }
+    const uint32_t k = (uint32_t)(i & 15);
+    const uint32_t w = k < 8 ? (k < 4 ? chunk.x : chunk.y) : (k < 12 ? chunk.z : chunk.w);
+    return (w >> (8 * (k & 3))) & 0xFFu;
   };
   uint32_t cr;
   uint64_t cc, ce;
@@ -78,7 +91,7 @@ __device__ __forceinline__ uint64_t probe(const Block* __restrict__ B, uint64_t 
     uint64_t e = 64 * rb + (uint64_t)select64(w, k);
     start = e + 1 > q ? e + 1 : q;
   }
-  return scan_run(B, nblocks, start, rem);
+  return scan_run(B, nblocks, start, rem, b, hdr.y);
 }
 
 __global__ void __launch_bounds__(256) k_bulk_get(Geom g, const uint64_t* __restrict__ keys,
