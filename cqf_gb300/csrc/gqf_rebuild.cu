@@ -309,35 +309,44 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
     }
     // now the keys of quotient q are kg[q ? kcnt(q-1) : 0, kcnt(q))
 
-    // ---- rank tables of the current image
-    if (wid == 0) {
-      constexpr int per = (WB + 31) / 32;
-      int a = lane * per, b = min(a + per, WB);
-      int so = 0, sr = 0;
-      for (int w = a; w < b; w++) {
-        if (w < wq_words) so += __popcll(C.occ(w));
-        if (w < wb) sr += __popcll(runs_after_c0(C, w));
+    // ---- rank tables of the current image: per window word, the occupied
+    // quotients and the runends after c0 before it (one packed block scan)
+    {
+      int packed = 0;
+      if (tid < WB) {
+        const int co = tid < wq_words ? __popcll(C.occ(tid)) : 0;
+        const int cr = tid < wb ? __popcll(runs_after_c0(C, tid)) : 0;
+        packed = co | (cr << 16);
       }
-      int io = so, ir = sr;
-      for (int o = 1; o < 32; o <<= 1) {
-        int t1 = __shfl_up_sync(0xffffffffu, io, o), t2 = __shfl_up_sync(0xffffffffu, ir, o);
-        if (lane >= o) { io += t1; ir += t2; }
+      int tot;
+      const int ex = scan_sum<NT>(packed, sa, &tot);
+      if (tid < WB) {
+        orank[tid] = (uint16_t)(ex & 0xFFFF);
+        rrank[tid] = (uint16_t)(ex >> 16);
       }
-      int eo = io - so, er = ir - sr;
-      for (int w = a; w < b; w++) {
-        orank[w] = (uint16_t)eo;
-        rrank[w] = (uint16_t)er;
-        if (w < wq_words) eo += __popcll(C.occ(w));
-        if (w < wb) er += __popcll(runs_after_c0(C, w));
-      }
-      if (lane == 31) { s_i[0] = ir; s_i[1] = io; }  // visible runends, occupied quotients
+      if (tid == 0) { s_i[0] = tot >> 16; s_i[1] = tot & 0xFFFF; }  // visible runends, occupied quotients
     }
     __syncthreads();
     const int nvis = s_i[0], nold = s_i[1];
-    for (int sl = tid; sl < wslots; sl += NT) {
-      unsigned long long rw = runs_after_c0(C, sl >> 6);
-      if ((rw >> (sl & 63)) & 1ULL)
-        rpos[rrank[sl >> 6] + __popcll(rw & ((1ULL << (sl & 63)) - 1ULL))] = (uint16_t)sl;
+    // Each thread owns QPT consecutive slots / quotients from here on, so
+    // ranks, run ends and shifts carry from one to the next in registers.
+    const int ca = tid * QPT;
+    {  // rpos[k] = the k-th runend after c0, for this thread's slots
+      const int cb = min(ca + QPT, wslots);
+      int x = ca;
+      while (x < cb) {
+        const int w = x >> 6;
+        const int xe = min(cb, 64 * w + 64);
+        unsigned long long m = runs_after_c0(C, w);
+        int k = rrank[w] + __popcll(m & ((1ULL << (x & 63)) - 1ULL));
+        m &= ~0ULL << (x & 63);
+        if (xe < 64 * w + 64) m &= (1ULL << (xe & 63)) - 1ULL;
+        while (m) {
+          rpos[k++] = (uint16_t)(64 * w + __ffsll((long long)m) - 1);
+          m &= m - 1;
+        }
+        x = xe;
+      }
     }
     __syncthreads();
 
@@ -347,27 +356,8 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       return (int)orank[q >> 6] + __popcll(C.occ(q >> 6) & ((1ULL << (q & 63)) - 1ULL));
     };
 
-    // ---- pass A: old run of every quotient (uniform across lanes)
-    for (int q = tid; q < win_q; q += NT) {
-      int len = 0;
-      if ((C.occ(q >> 6) >> (q & 63)) & 1ULL) {
-        const int k = rank_of(q);
-        const int e = runpos(k);
-        const int s = max(q, (k ? runpos(k - 1) : c0) + 1);
-        len = e - s + 1;
-        delta[k] = (int16_t)s;
-        const int last = min(e, wslots - 1);
-        for (int x = s; x <= last;) {  // mark the run's slots
-          const int hi = min(last, x | 31);
-          const int hb = hi & 31;
-          atomicOr(&used[x >> 5], (hb == 31 ? ~0u : ((2u << hb) - 1u)) & (~0u << (x & 31)));
-          x = hi + 1;
-        }
-      }
-      pref[q] = (uint16_t)len;
-    }
-    __syncthreads();
-    // ---- merge tasks: one per touched quotient (the first key of each group)
+    // ---- merge tasks: new length of every touched quotient (first key of
+    // each group), before the positions are scanned
     bool my_defer = false;
     for (int i = tid; i < nk; i += NT) {
       const uint32_t q = kg[i] >> 8;
@@ -379,7 +369,7 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       if (occ) {
         const int k = rank_of((int)q);
         e = runpos(k);
-        s = delta[k];
+        s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
       }
       if (occ && e >= win_valid) {
         my_defer = true;
@@ -394,41 +384,54 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       pref[q] = (uint16_t)merge_run<DEL, false>(C, occ, s, e, kg, ks, ke, N, 0);
     }
     if (__syncthreads_or(my_defer)) { deferred = true; break; }
-    // ---- new occupancy: 32 quotients per warp ballot
-    for (int q0 = 0; q0 < WIN; q0 += NT) {
-      const int q = q0 + tid;
-      const unsigned bal = __ballot_sync(0xffffffffu, q < win_q && pref[q] > 0);
-      const int qw = q0 + wid * 32;
-      if (lane == 0 && bal) atomicOr(reinterpret_cast<uint32_t*>(&nocc[qw >> 6]) + ((qw >> 5) & 1), bal);
-    }
-    __syncthreads();
 
-    // ---- run positions: one block-wide max-plus scan over the quotients
+    // ---- this thread's quotients: old runs, new lengths, composed max-plus map
+    const int qb_ = min(ca + QPT, win_q);
+    const int k0 = ca < win_q ? rank_of(ca) : nold;
+    int fa = kNeg, fb = 0;
     {
-      const int qa = tid * QPT, qb = min(qa + QPT, win_q);
-      int fa = kNeg, fb = 0;
-      for (int q = qa; q < qb; q++) {
-        int len = pref[q];
+      int k = k0;
+      int pe = k ? runpos(k - 1) : c0;
+      int ne = runpos(k);  // end of the next old run
+      unsigned long long ow = 0, tw = 0;
+      int cw = -1;
+      uint32_t ubits = 0;  // used-slot bits of 32-bit word uw
+      int uw = -1;
+      for (int q = ca; q < qb_; q++) {
+        if ((q >> 6) != cw) {
+          cw = q >> 6;
+          ow = C.occ(cw);
+          tw = q < nq ? tch[cw] : 0ULL;
+        }
+        int len = 0;
+        if ((ow >> (q & 63)) & 1ULL) {
+          const int e = ne;
+          ne = runpos(k + 1);
+          const int s = max(q, pe + 1);
+          len = e - s + 1;
+          delta[k] = (int16_t)s;
+          const int last = min(e, wslots - 1);
+          for (int x = s; x <= last; x++) {  // mark the run's slots
+            if ((x >> 5) != uw) {
+              if (ubits) atomicOr(&used[uw], ubits);
+              uw = x >> 5;
+              ubits = 0;
+            }
+            ubits |= 1u << (x & 31);
+          }
+          pe = e;
+          k++;
+        }
+        if ((tw >> (q & 63)) & 1ULL) len = pref[q];
+        pref[q] = (uint16_t)len;
         if (len > 0) { fa = max(q + len - 1, fa + len); fb += len; }
       }
-      scan_maps<NT>(fa, fb, sa, sb);
-      int x = max(fa, c0 + fb);  // end of all runs before qa
-      for (int q = qa; q < qb; q++) {
-        int len = pref[q];
-        if (len > 0) x = max(q + len - 1, x + len);
-        pref[q] = (uint16_t)(x + 1);
-      }
-    }
-    __syncthreads();
-    {
-      const int e_old = nold ? runpos(nold - 1) : c0;
-      const int e_new = (int)pref[win_q - 1] - 1;
-      // A change that reaches the window's end would move runs this CTA does
-      // not hold (or overflow the table): leave the region to the serial pass.
-      if (e_new != e_old && max(e_new, e_old) >= win_valid) { deferred = true; break; }
+      if (ubits) atomicOr(&used[uw], ubits);
     }
 
-    // ---- build the next image: clear, keep the previous region's spill
+    // ---- run positions: one block-wide max-plus scan over the quotients
+    scan_maps<NT>(fa, fb, sa, sb);
+    // ---- clear the next image; keep the previous region's spill
     {
       uint4* dst = reinterpret_cast<uint4*>(N.p);
       for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
@@ -440,17 +443,52 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       N.run(w) = nb >= 63 ? C.run(w) : (C.run(w) & ((2ULL << nb) - 1ULL));
     }
     __syncthreads();
-    // ---- pass B: shift of every untouched run, runends of the new layout
-    for (int q = tid; q < win_q; q += NT) {
-      const bool no = (nocc[q >> 6] >> (q & 63)) & 1ULL;
-      const int ne = (int)pref[q] - 1;
-      if (no && ne < wslots) N.set_end(ne);
-      if ((C.occ(q >> 6) >> (q & 63)) & 1ULL) {
-        const bool touched = q < nq && ((tch[q >> 6] >> (q & 63)) & 1ULL);
-        const int k = rank_of(q);
-        const int ns = max(q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
-        delta[k] = touched ? kTouched : (int16_t)(ns - delta[k]);
+    // ---- apply: new ends, runend bits, occupancy, shift of every old run
+    {
+      int x = max(fa, c0 + fb);  // end of all runs before this thread's first quotient
+      int k = k0;
+      unsigned long long occ_bits = 0, ow = 0, tw = 0;
+      int occ_word = ca >> 6, cw = -1;
+      unsigned long long ebits = 0;  // new runend bits of window word ew
+      int ew = -1;
+      for (int q = ca; q < qb_; q++) {
+        if ((q >> 6) != cw) {
+          if (cw >= 0 && occ_bits) atomicOr(&nocc[occ_word], occ_bits);
+          occ_bits = 0;
+          cw = occ_word = q >> 6;
+          ow = C.occ(cw);
+          tw = q < nq ? tch[cw] : 0ULL;
+        }
+        const int len = pref[q];
+        const int ns = max(q, x + 1);
+        if (len > 0) {
+          x = ns + len - 1;
+          occ_bits |= 1ULL << (q & 63);
+          if (x < wslots) {
+            if ((x >> 6) != ew) {
+              if (ebits) atomicOr(&N.run(ew), ebits);
+              ew = x >> 6;
+              ebits = 0;
+            }
+            ebits |= 1ULL << (x & 63);
+          }
+        }
+        if ((ow >> (q & 63)) & 1ULL) {
+          delta[k] = ((tw >> (q & 63)) & 1ULL) ? kTouched : (int16_t)(ns - delta[k]);
+          k++;
+        }
+        pref[q] = (uint16_t)(x + 1);
       }
+      if (occ_bits) atomicOr(&nocc[occ_word], occ_bits);
+      if (ebits) atomicOr(&N.run(ew), ebits);
+    }
+    __syncthreads();
+    {
+      const int e_old = nold ? runpos(nold - 1) : c0;
+      const int e_new = (int)pref[win_q - 1] - 1;
+      // A change that reaches the window's end would move runs this CTA does
+      // not hold (or overflow the table): leave the region to the serial pass.
+      if (e_new != e_old && max(e_new, e_old) >= win_valid) { deferred = true; break; }
     }
     // ---- merge tasks again, now writing the touched runs at their new start
     for (int i = tid; i < nk; i += NT) {
@@ -468,17 +506,30 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
       merge_run<DEL, true>(C, occ, s, e, kg, ks, ke, N, ns);
     }
-    __syncthreads();
-    // ---- slot pass: every untouched run's bytes move by their run's shift
-    for (int sl = tid; sl < wslots; sl += NT) {
-      if (!((used[sl >> 5] >> (sl & 31)) & 1u)) continue;
-      const int w = sl >> 6;
-      const int k = rrank[w] + __popcll(runs_after_c0(C, w) & ((1ULL << (sl & 63)) - 1ULL));
-      const int d = delta[k];
-      if (d == kTouched) continue;
-      const int t = sl + d;
-      if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
+    // ---- slot pass: this thread's slots move by their run's shift
+    {
+      const int cb = min(ca + QPT, wslots);
+      if (ca < cb) {
+        int w = ca >> 6;
+        unsigned long long m = runs_after_c0(C, w);
+        int k = rrank[w] + __popcll(m & ((1ULL << (ca & 63)) - 1ULL));
+        for (int sl = ca; sl < cb; sl++) {
+          if ((sl >> 6) != w) {
+            w = sl >> 6;
+            m = runs_after_c0(C, w);
+          }
+          if ((used[sl >> 5] >> (sl & 31)) & 1u) {
+            const int d = delta[k];
+            if (d != kTouched) {
+              const int t = sl + d;
+              if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
+            }
+          }
+          k += (int)((m >> (sl & 63)) & 1ULL);
+        }
+      }
     }
+    __syncthreads();
     // ---- block headers: occupieds and offsets
     for (int w = tid; w < wb; w += NT) {
       N.occ(w) = w < wq_words ? nocc[w] : 0ULL;
