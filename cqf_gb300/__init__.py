@@ -57,6 +57,8 @@ SIGNATURES = {
     "gqf_bulk_delete_async": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_get_async": (_int, [_vp, _u64, _vp, _vp, _u8, _vp]),
     "gqf_bulk_insert_noalloc": (_int, [_vp, _u64, _vp, _u8, _vp]),
+    "gqf_bulk_insert_kmers": (_int, [_vp, _vp, _u64, _u32, _u32, _vp]),
+    "gqf_kmers_extract": (_int, [_vp, _u64, _u32, _u32, _vp, _vp]),
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
@@ -211,6 +213,14 @@ class QF:
         n = keys.numel() if n is None else n
         self._ok(self.L.gqf_bulk_insert_noalloc(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
 
+    def bulk_insert_reduce_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
+        self._ok(self.L.gqf_bulk_insert_reduce_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
+
+    def bulk_insert_kmers(self, reads, k: int, stream=None):
+        """Counts the canonical k-mers of a device uint8 tensor [nreads, read_len]."""
+        nreads, read_len = reads.shape
+        self._ok(self.L.gqf_bulk_insert_kmers(self.h, _ptr(reads), nreads, read_len, k, _stream_ptr(stream)))
+
     def bulk_delete_async(self, keys, n, flags=QF_NO_LOCK, stream=None):
         self._ok(self.L.gqf_bulk_delete_async(self.h, n, _ptr(keys), flags, _stream_ptr(stream)))
 
@@ -282,6 +292,13 @@ class QF:
     def _ok(self, rc: int):
         if rc != 0:
             raise RuntimeError(last_error())
+
+
+def kmers_extract(reads, k: int, out, stream=None):
+    """out[read * nk + pos] = canonical k-mer (uint64; all ones = skipped window)."""
+    nreads, read_len = reads.shape
+    if load().gqf_kmers_extract(_ptr(reads), nreads, read_len, k, _ptr(out), _stream_ptr(stream)) != 0:
+        raise RuntimeError(last_error())
 
 
 def launch_count() -> int:

@@ -50,6 +50,9 @@ struct HostFilter {
   uint64_t key_cap = 0;
   uint32_t region_cap = 0;
   bool counts_alloc = false;
+  uint64_t* merge_h = nullptr;  // bulk_insert_reduce: merged (hash, count) pairs
+  uint32_t* merge_c = nullptr;
+  uint64_t merge_cap = 0;
   uint8_t* packed = nullptr;  // export / import staging
   // phase timers (CUDA events on the launching stream), off by default
   bool prof = false;
@@ -115,6 +118,7 @@ int auto_log_region(int nbits) {
 uint32_t* status_ptr(HostFilter* f) { return reinterpret_cast<uint32_t*>(f->aux); }
 unsigned long long* misses_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 64); }
 unsigned long long* stats_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 128); }
+unsigned long long* merged_ptr(HostFilter* f) { return reinterpret_cast<unsigned long long*>(f->aux + 192); }
 
 uint32_t nregions_for(const HostFilter* f, int log_region) {
   uint64_t n = f->h.nslots >> log_region;
@@ -161,6 +165,61 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
   f->part.log_region = f->log_region;
   f->part.stats = stats_ptr(f);
   return true;
+}
+
+bool ensure_merge(HostFilter* f, uint64_t nkeys, cudaStream_t st) {
+  if (nkeys <= f->merge_cap) return true;
+  const uint64_t cap = nkeys + nkeys / 8 + 1024;
+  if (f->merge_h) cudaFreeAsync(f->merge_h, st);
+  if (f->merge_c) cudaFreeAsync(f->merge_c, st);
+  f->merge_h = nullptr;
+  f->merge_c = nullptr;
+  f->merge_cap = 0;
+  if (!ck(cudaMallocAsync((void**)&f->merge_h, cap * sizeof(uint64_t), st), "cudaMallocAsync merge") ||
+      !ck(cudaMallocAsync((void**)&f->merge_c, cap * sizeof(uint32_t), st), "cudaMallocAsync merge"))
+    return false;
+  f->merge_cap = cap;
+  return true;
+}
+
+// bulk_insert_reduce: equal hashes are merged into (hash, count) pairs first
+// (gqf_reduce.cu), then partitioned and rebuilt with counts.  With reads,
+// the keys are the reads' canonical k-mers instead of keys[].
+int do_bulk_reduce(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, cudaStream_t st,
+                   const uint8_t* reads = nullptr, uint64_t nreads = 0, uint32_t read_len = 0,
+                   uint32_t k = 0) {
+  std::lock_guard<std::mutex> lk(f->mu);
+  if (reads) {
+    if (!kmer_shape_ok(nreads, read_len, k)) {
+      set_err("k-mers: need 1 <= k <= 32 and k <= read_len <= k + 4095");
+      return -1;
+    }
+    n = nreads * (read_len - k + 1);
+  } else if (!keys && n) {
+    set_err("null keys");
+    return -1;
+  }
+  if (n == 0) return 0;
+  if (!ensure_partition(f, n, true, st) || !ensure_merge(f, n, st)) return -1;
+  Partition p = f->part;
+  const int key_is_hash = (flags & QF_KEY_IS_HASH) ? 1 : 0;
+  {
+    PhaseTimer t(f, GQF_PROF_PARTITION, st, n);
+    if (!ck(cudaMemsetAsync(merged_ptr(f), 0, sizeof(unsigned long long), st), "memset") ||
+        !ck(reads ? launch_merge_kmers(f->g, reads, nreads, read_len, k, f->merge_h, f->merge_c,
+                                       merged_ptr(f), st)
+                  : launch_merge_tiles(f->g, keys, n, key_is_hash, f->merge_h, f->merge_c, merged_ptr(f),
+                                       status_ptr(f), st), "merge_tiles") ||
+        !ck(launch_partition_counted(f->g, p, f->merge_h, f->merge_c, n, merged_ptr(f), 1, status_ptr(f), st),
+            "partition") ||
+        !ck(launch_merge_regions(p, st), "merge_regions"))
+      return -1;
+  }
+  {
+    PhaseTimer t(f, GQF_PROF_INSERT, st, n);
+    if (!ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st), "rebuild")) return -1;
+  }
+  return 0;
 }
 
 int do_bulk(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, Op op, cudaStream_t st) {
@@ -279,6 +338,8 @@ void qf_destroy_device(QF* qf) {
   for (cudaEvent_t e : f->spare) cudaEventDestroy(e);
   if (f->part.keys) cudaFree(f->part.keys);
   if (f->part.counts) cudaFree(f->part.counts);
+  if (f->merge_h) cudaFree(f->merge_h);
+  if (f->merge_c) cudaFree(f->merge_c);
   if (f->part.region_count) cudaFree(f->part.region_count);
   if (f->packed) cudaFree(f->packed);
   cudaFree(f->h.blocks);
@@ -292,11 +353,11 @@ void bulk_insert(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
   if (HostFilter* f = lookup(qf)) do_bulk(f, nvals, keys, flags, Op::kInsert, f->stream);
 }
 
-// Duplicates inside a batch are merged into counters by the rebuild itself,
-// so the reduce variant needs no separate sort + reduce_by_key
-// (src/gqf.cu:3261-3279).
+// Equal hashes are merged in shared-memory tables instead of the reference's
+// sort + reduce_by_key (src/gqf.cu:3261-3279); the counted rebuild then adds
+// each distinct hash once with its multiplicity.
 void bulk_insert_reduce(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
-  if (HostFilter* f = lookup(qf)) do_bulk(f, nvals, keys, flags, Op::kInsert, f->stream);
+  if (HostFilter* f = lookup(qf)) do_bulk_reduce(f, nvals, keys, flags, f->stream);
 }
 
 void bulk_delete(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags) {
@@ -372,7 +433,31 @@ int gqf_bulk_insert_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t 
 int gqf_bulk_insert_reduce_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags,
                                  void* stream) {
   HostFilter* f = lookup(qf);
-  return f ? do_bulk(f, nvals, keys, flags, Op::kInsert, (cudaStream_t)stream) : -1;
+  return f ? do_bulk_reduce(f, nvals, keys, flags, (cudaStream_t)stream) : -1;
+}
+
+int gqf_bulk_insert_kmers(QF* qf, const uint8_t* reads, uint64_t nreads, uint32_t read_len, uint32_t k,
+                          void* stream) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  if (!reads && nreads) {
+    set_err("null reads");
+    return -1;
+  }
+  return do_bulk_reduce(f, 0, nullptr, 0, (cudaStream_t)stream, reads, nreads, read_len, k);
+}
+
+int gqf_kmers_extract(const uint8_t* reads, uint64_t nreads, uint32_t read_len, uint32_t k, uint64_t* out,
+                      void* stream) {
+  if (!kmer_shape_ok(nreads, read_len, k)) {
+    set_err("k-mers: need 1 <= k <= 32 and k <= read_len <= k + 4095");
+    return -1;
+  }
+  if (nreads && (!reads || !out)) {
+    set_err("null reads or output");
+    return -1;
+  }
+  return ck(launch_kmers(reads, nreads, read_len, k, out, (cudaStream_t)stream), "kmers") ? 0 : -1;
 }
 
 int gqf_bulk_delete_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream) {

@@ -66,6 +66,33 @@ cudaError_t launch_bulk_get_misses(const Geom& g, const uint64_t* keys, uint64_t
 cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
                              int key_is_hash, uint32_t* status, cudaStream_t st);
 
+// The same for (hash, count) pairs whose number n_dev the device holds (n
+// bounds it): hashes are taken as they are, counts land in p.counts.
+cudaError_t launch_partition_counted(const Geom& g, const Partition& p, const uint64_t* keys,
+                                     const uint32_t* counts, uint64_t n, const unsigned long long* n_dev,
+                                     int key_is_hash, uint32_t* status, cudaStream_t st);
+
+// Duplicate merging for bulk_insert_reduce.  Tile pass: each CTA merges the
+// equal hashes of a tile of keys in a shared-memory table and appends
+// (hash, count) pairs at out_*[*n_out].  Region pass: regions left with more
+// pairs than one rebuild round takes are merged again in place, shrinking
+// p.region_count.
+cudaError_t launch_merge_tiles(const Geom& g, const uint64_t* keys, uint64_t n, int key_is_hash,
+                               uint64_t* out_hashes, uint32_t* out_counts, unsigned long long* n_out,
+                               uint32_t* status, cudaStream_t st);
+cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st);
+
+// K-mers of fixed-length reads (read_len bytes each, ACGT in either case):
+// the tile pass over the canonical k-mers (2-bit packed, first base in the
+// high bits), hashed like keys; and a plain extraction into out[read * nk +
+// pos], nk = read_len - k + 1, ~0 for windows holding another byte.
+bool kmer_shape_ok(uint64_t nreads, uint32_t read_len, uint32_t k);
+cudaError_t launch_merge_kmers(const Geom& g, const uint8_t* reads, uint64_t nreads, uint32_t read_len,
+                               uint32_t k, uint64_t* out_hashes, uint32_t* out_counts,
+                               unsigned long long* n_out, cudaStream_t st);
+cudaError_t launch_kmers(const uint8_t* reads, uint64_t nreads, uint32_t read_len, uint32_t k, uint64_t* out,
+                         cudaStream_t st);
+
 // Even regions, then odd regions, then the serial fallback for regions whose
 // rebuild window was exceeded.
 cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_filter* dqf,

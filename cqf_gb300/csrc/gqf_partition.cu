@@ -29,10 +29,14 @@ __device__ __forceinline__ bool hash_key(const Geom& g, const uint64_t* keys, ui
   return true;
 }
 
+// n_dev, when given, holds the key count instead of n (a count produced on
+// the device by the duplicate-merging pass).
 __global__ void __launch_bounds__(256) k_part_count(Geom g, const uint64_t* __restrict__ keys,
-                                                    uint64_t n, int key_is_hash, int shift,
+                                                    uint64_t n, const unsigned long long* n_dev,
+                                                    int key_is_hash, int shift,
                                                     uint32_t* __restrict__ region_count,
                                                     uint32_t* status) {
+  if (n_dev) n = min(n, (uint64_t)*n_dev);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t nr = (n + 31) & ~31ULL;
   const unsigned lane = threadIdx.x & 31;
@@ -83,9 +87,13 @@ __global__ void __launch_bounds__(1024) k_part_scan(const uint32_t* __restrict__
 }
 
 __global__ void __launch_bounds__(256) k_part_scatter(Geom g, const uint64_t* __restrict__ keys,
-                                                      uint64_t n, int key_is_hash, int shift,
+                                                      uint64_t n, const unsigned long long* n_dev,
+                                                      const uint32_t* __restrict__ counts,
+                                                      int key_is_hash, int shift,
                                                       uint32_t* __restrict__ cursor,
-                                                      uint32_t* __restrict__ out) {
+                                                      uint32_t* __restrict__ out,
+                                                      uint32_t* __restrict__ out_counts) {
+  if (n_dev) n = min(n, (uint64_t)*n_dev);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t nr = (n + 31) & ~31ULL;
   const unsigned lane = threadIdx.x & 31;
@@ -99,7 +107,11 @@ __global__ void __launch_bounds__(256) k_part_scatter(Geom g, const uint64_t* __
     uint32_t base = 0;
     if (ok && lane == leader) base = atomicAdd(&cursor[r], (uint32_t)__popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (ok) out[base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)(h & local_mask);
+    if (ok) {
+      const uint32_t at = base + __popc(peers & ((1u << lane) - 1u));
+      out[at] = (uint32_t)(h & local_mask);
+      if (counts) out_counts[at] = counts[i];
+    }
   }
 }
 
@@ -121,17 +133,24 @@ int grid_for(uint64_t n) {
 
 cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
                              int key_is_hash, uint32_t* status, cudaStream_t st) {
+  return launch_partition_counted(g, p, keys, nullptr, n, nullptr, key_is_hash, status, st);
+}
+
+cudaError_t launch_partition_counted(const Geom& g, const Partition& p, const uint64_t* keys,
+                                     const uint32_t* counts, uint64_t n, const unsigned long long* n_dev,
+                                     int key_is_hash, uint32_t* status, cudaStream_t st) {
   const int shift = 8 + p.log_region;
   cudaError_t e = cudaMemsetAsync(p.region_count, 0, (p.nregions + 1) * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (n) {
-    k_part_count<<<grid_for(n), 256, 0, st>>>(g, keys, n, key_is_hash, shift, p.region_count, status);
+    k_part_count<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, key_is_hash, shift, p.region_count, status);
     count_launch();
   }
   k_part_scan<<<1, 1024, 0, st>>>(p.region_count, p.region_start, p.cursor, p.nregions);
   count_launch();
   if (n) {
-    k_part_scatter<<<grid_for(n), 256, 0, st>>>(g, keys, n, key_is_hash, shift, p.cursor, p.keys);
+    k_part_scatter<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, counts, key_is_hash, shift, p.cursor,
+                                                p.keys, p.counts);
     count_launch();
   }
   return cudaGetLastError();

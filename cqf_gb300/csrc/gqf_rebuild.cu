@@ -41,7 +41,7 @@ struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 3; };
 template <>
 struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 1; };
 
-template <int LOGS>
+template <int LOGS, bool CNT>
 struct Lay {
   static constexpr int NT = 256;
   static constexpr int REG = 1 << LOGS;
@@ -68,7 +68,8 @@ struct Lay {
   static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
   static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
   static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;     // u16[WB + 8]
-  static constexpr int BYTES = OFF_RRANK + (WB + 8) * 2;
+  static constexpr int OFF_KN = (OFF_RRANK + (WB + 8) * 2 + 3) & ~3;  // u32[KMAX] key counts (CNT)
+  static constexpr int BYTES = OFF_KN + (CNT ? KMAX * 4 : 0);
 };
 
 constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
@@ -82,18 +83,14 @@ struct Img {
   __device__ unsigned long long& run(int w) const { return *reinterpret_cast<unsigned long long*>(p + w * 96 + 8); }
   __device__ uint32_t& off(int w) const { return *reinterpret_cast<uint32_t*>(p + w * 96 + 16); }
   __device__ int is_end(int i) const { return (int)((run(i >> 6) >> (i & 63)) & 1ULL); }
-  __device__ void set_end(int i) const {
-    uint32_t* w = reinterpret_cast<uint32_t*>(p + (i >> 6) * 96 + 8) + ((i >> 5) & 1);
-    atomicOr(w, 1u << (i & 31));
-  }
 };
 
-// Merge one run's old counters with the run's new keys (sorted by remainder,
-// one occurrence each) and return the new run length; with WRITE, also emit
-// the bytes at out[pos..].
+// Merge one run's old counters with the run's new keys (sorted by remainder;
+// each key counts once, or cnts[j] times when cnts is given) and return the
+// new run length; with WRITE, also emit the bytes at out[pos..].
 template <bool DEL, bool WRITE>
-__device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* keys, int ki, int kj,
-                         Img out, int pos) {
+__device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* keys, const uint32_t* cnts,
+                         int ki, int kj, Img out, int pos) {
   auto get = [&](uint64_t i) -> uint64_t { return cur.slot((int)i); };
   auto end = [&](uint64_t i) -> int { return cur.is_end((int)i); };
   const uint64_t lim = (uint64_t)e + 1;  // the walk never leaves the run [s, e]
@@ -113,7 +110,7 @@ __device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* ke
     if (j < kj) {
       nrem = keys[j] & 255u;
       while (jn < kj && (keys[jn] & 255u) == nrem) {
-        ncnt++;
+        ncnt += cnts ? cnts[jn] : 1u;
         jn++;
       }
     }
@@ -208,10 +205,12 @@ __device__ int scan_sum(int v, int* tmp, int* total) {
   return r;
 }
 
-template <int LOGS, bool DEL>
-__global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partition p, int parity,
-                                                                   uint32_t* status) {
-  using L = Lay<LOGS>;
+// CNT: the batch carries a multiplicity per key (p.counts), as produced by
+// the duplicate-merging pass of bulk_insert_reduce.
+template <int LOGS, bool DEL, bool CNT>
+__global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom g, Partition p, int parity,
+                                                                             uint32_t* status) {
+  using L = Lay<LOGS, CNT>;
   constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
   extern __shared__ __align__(128) uint8_t sm[];
   __shared__ int s_i[8];
@@ -219,9 +218,9 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
 
   const uint32_t r = 2 * blockIdx.x + parity;
   if (r >= p.nregions) return;
-  const uint32_t kbeg = p.region_start[r], kend = p.region_start[r + 1];
+  const uint32_t kbeg = p.region_start[r], kend = kbeg + p.region_count[r];
   if (kbeg == kend) return;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int tid = threadIdx.x;
 
   const uint64_t base = (uint64_t)r << LOGS;
   const uint64_t bw0 = base >> 6;
@@ -242,6 +241,7 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
   unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
   uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
   uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
+  uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
 
   // ---- stage the window (wb blocks of 96 bytes) into image 0
   {
@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       uint32_t sh = (q & 1) * 16;
       uint32_t old = atomicAdd(&kc[q >> 1], 1u << sh);
       kg[(old >> sh) & 0xFFFFu] = key;
+      if (CNT) kn[(old >> sh) & 0xFFFFu] = p.counts[kr + i];
     }
     // now the keys of quotient q are kg[q ? kcnt(q-1) : 0, kcnt(q))
 
@@ -377,11 +378,17 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
       }
       for (int a = ks + 1; a < ke; a++) {  // the quotient's keys by remainder
         const uint32_t v = kg[a];
+        const uint32_t vc = CNT ? kn[a] : 0u;
         int b = a;
-        while (b > ks && kg[b - 1] > v) { kg[b] = kg[b - 1]; b--; }
+        while (b > ks && kg[b - 1] > v) {
+          kg[b] = kg[b - 1];
+          if (CNT) kn[b] = kn[b - 1];
+          b--;
+        }
         kg[b] = v;
+        if (CNT) kn[b] = vc;
       }
-      pref[q] = (uint16_t)merge_run<DEL, false>(C, occ, s, e, kg, ks, ke, N, 0);
+      pref[q] = (uint16_t)merge_run<DEL, false>(C, occ, s, e, kg, kn, ks, ke, N, 0);
     }
     if (__syncthreads_or(my_defer)) { deferred = true; break; }
 
@@ -504,7 +511,7 @@ __global__ void __launch_bounds__(256, Cfg<LOGS>::MINB) k_rebuild(Geom g, Partit
         s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
       }
       const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
-      merge_run<DEL, true>(C, occ, s, e, kg, ks, ke, N, ns);
+      merge_run<DEL, true>(C, occ, s, e, kg, kn, ks, ke, N, ns);
     }
     // ---- slot pass: this thread's slots move by their run's shift
     {
@@ -592,8 +599,8 @@ __global__ void k_fallback(quotient_filter* dqf, Partition p, int del, uint32_t*
   const int shift = 8 + p.log_region;
   for (uint32_t i = 0; i < n; i++) {
     uint32_t r = ids[i];
-    if (p.stats) p.stats[1] += p.region_start[r + 1] - p.region_start[r];
-    for (uint32_t k = p.region_start[r]; k < p.region_start[r + 1]; k++) {
+    if (p.stats) p.stats[1] += p.region_count[r];
+    for (uint32_t k = p.region_start[r]; k < p.region_start[r] + p.region_count[r]; k++) {
       uint64_t h = ((uint64_t)r << shift) | p.keys[k];
       uint64_t c = p.counts ? p.counts[k] : 1;
       if (del) {
@@ -606,25 +613,33 @@ __global__ void k_fallback(quotient_filter* dqf, Partition p, int del, uint32_t*
   }
 }
 
+template <int LOGS, bool DEL, bool CNT>
+void configure() {
+  static bool done = false;  // per instantiation
+  if (done) return;
+  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       Lay<LOGS, CNT>::BYTES);
+  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  done = true;
+}
+
 template <int LOGS>
 cudaError_t run_phases(const Geom& g, const Partition& p, Op op, uint32_t* status, cudaStream_t st) {
-  using L = Lay<LOGS>;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_rebuild<LOGS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
-    cudaFuncSetAttribute(k_rebuild<LOGS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
-    cudaFuncSetAttribute(k_rebuild<LOGS, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_rebuild<LOGS, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    configured = true;
-  }
+  const bool cnt = p.counts != nullptr;
+  if (op == Op::kDelete && cnt) return cudaErrorInvalidValue;  // deletes carry no counts
+  if (op == Op::kDelete) configure<LOGS, true, false>();
+  else if (cnt) configure<LOGS, false, true>();
+  else configure<LOGS, false, false>();
   const uint32_t half = (p.nregions + 1) / 2;
   for (int parity = 0; parity < 2; parity++) {
     uint32_t grid = parity ? p.nregions / 2 : half;
     if (!grid) continue;
     if (op == Op::kDelete)
-      k_rebuild<LOGS, true><<<grid, L::NT, L::BYTES, st>>>(g, p, parity, status);
+      k_rebuild<LOGS, true, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, status);
+    else if (cnt)
+      k_rebuild<LOGS, false, true><<<grid, 256, Lay<LOGS, true>::BYTES, st>>>(g, p, parity, status);
     else
-      k_rebuild<LOGS, false><<<grid, L::NT, L::BYTES, st>>>(g, p, parity, status);
+      k_rebuild<LOGS, false, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, status);
     count_launch();
   }
   return cudaGetLastError();
@@ -634,9 +649,9 @@ cudaError_t run_phases(const Geom& g, const Partition& p, Op op, uint32_t* statu
 
 size_t rebuild_smem_bytes(int log_region) {
   switch (log_region) {
-    case 11: return Lay<11>::BYTES;
-    case 12: return Lay<12>::BYTES;
-    case 13: return Lay<13>::BYTES;
+    case 11: return Lay<11, false>::BYTES;
+    case 12: return Lay<12, false>::BYTES;
+    case 13: return Lay<13, false>::BYTES;
   }
   return 0;
 }

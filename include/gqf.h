@@ -76,7 +76,9 @@ void qf_destroy_device(QF* qf);
 /* include/gqf.cuh:109.  Inserts nvals device-resident keys (count 1 each). */
 void bulk_insert(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags);
 
-/* include/gqf.cuh:112.  Same result as bulk_insert; for skewed batches. */
+/* include/gqf.cuh:112.  Same result as bulk_insert; for skewed batches:
+ * equal keys are merged into counts on the device before they are inserted
+ * (the reference sorts and runs reduce_by_key, src/gqf.cu:3238-3313). */
 void bulk_insert_reduce(QF* qf, uint64_t nvals, uint64_t* keys, uint8_t flags);
 
 /* include/gqf.cuh:115.  Decrements each key's count by one (absent keys are
@@ -115,6 +117,22 @@ int gqf_bulk_insert_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t 
 int gqf_bulk_insert_reduce_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags,
                                  void* stream);
 int gqf_bulk_delete_async(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
+
+/* No counterpart in the reference's bulk API: its k-mer counting
+ * (src/gqf_verify.cu:117-245) cuts ASCII k-mers on the host and hashes each
+ * string.  Here the reads stay on the device: nreads fixed-length reads of
+ * read_len bytes (ACGT, either case), k in [1, 32], read_len - k + 1 <= 4096.
+ * Each k-mer is 2-bit packed (A=0 C=1 G=2 T=3, first base in the high bits)
+ * and canonicalised (the smaller of the k-mer and its reverse complement);
+ * windows holding another byte are skipped.
+ *   gqf_bulk_insert_kmers: bulk_insert_reduce of the reads' canonical k-mers.
+ *   gqf_kmers_extract:     out[read * (read_len - k + 1) + pos] = the k-mer at
+ *                          pos, or UINT64_MAX for a skipped window.
+ * reads and out are device pointers; stream as above.  Returns 0 or -1. */
+int gqf_bulk_insert_kmers(QF* qf, const uint8_t* reads, uint64_t nreads, uint32_t read_len, uint32_t k,
+                          void* stream);
+int gqf_kmers_extract(const uint8_t* reads, uint64_t nreads, uint32_t read_len, uint32_t k, uint64_t* out,
+                      void* stream);
 int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* returns, uint8_t flags,
                        void* stream);
 

@@ -312,3 +312,48 @@ def parse_dump(buf: np.ndarray):
     run = np.ascontiguousarray(blocks[:, 9:17]).view(np.uint64).reshape(-1)
     slots = blocks[:, 17:].copy()
     return meta, offsets, occ, run, slots
+
+
+_BASE_CODE = np.full(256, 255, dtype=np.uint8)
+for _c, _v in zip(b"ACGTacgt", (0, 1, 2, 3, 0, 1, 2, 3)):
+    _BASE_CODE[_c] = _v
+
+
+def canonical_kmers(reads: np.ndarray, k: int) -> np.ndarray:
+    """Canonical k-mers of fixed-length ASCII reads, uint64 [nreads * nk].
+
+    The reference cuts k-mers as substrings of each read line
+    (src/gqf_verify.cu:158-170); here each window is 2-bit packed (A=0 C=1
+    G=2 T=3, first base in the high bits) and replaced by the smaller of
+    itself and its reverse complement.  Windows holding a byte other than
+    ACGT (either case) give all ones.  Vectorised over reads."""
+    reads = np.ascontiguousarray(reads, dtype=np.uint8)
+    nreads, length = reads.shape
+    nk = length - k + 1
+    codes = _BASE_CODE[reads]
+    bad = codes == 255
+    c = np.where(bad, 0, codes).astype(np.uint64)
+    fw = np.zeros((nreads, nk), dtype=np.uint64)
+    rc = np.zeros((nreads, nk), dtype=np.uint64)
+    badw = np.zeros((nreads, nk), dtype=bool)
+    for j in range(k):
+        cj = c[:, j:j + nk]
+        fw = (fw << np.uint64(2)) | cj
+        rc = rc | ((np.uint64(3) - cj) << np.uint64(2 * j))
+        badw |= bad[:, j:j + nk]
+    out = np.minimum(fw, rc)
+    out[badw] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    return out.reshape(-1)
+
+
+def exact_counts(keys: np.ndarray, nbits: int, probe: np.ndarray) -> np.ndarray:
+    """Exact multiplicity of each probe key among keys, with keys identified
+    modulo 2^(nbits+8): hash_64 (src/hashutil.cu:132-140) reads only those
+    bits, so keys equal there share one counter in any filter."""
+    m = np.uint64((1 << (nbits + 8)) - 1)
+    u, cnt = np.unique(np.asarray(keys, dtype=np.uint64) & m, return_counts=True)
+    p = np.asarray(probe, dtype=np.uint64) & m
+    i = np.searchsorted(u, p)
+    i = np.minimum(i, max(0, u.size - 1))
+    hit = (u.size > 0) & (u[i] == p) if u.size else np.zeros(p.shape, dtype=bool)
+    return np.where(hit, cnt[i] if u.size else 0, 0).astype(np.uint64)
