@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-skew", action="store_true", help="skip the skewed-counting workloads")
     return ap.parse_args()
 
 
@@ -345,6 +346,13 @@ def run_gpu(args, wl, rank, world):
         qf.close()
         ref_cuda = run_ref_cuda(wl, keys, absent, ops, value, torch)
 
+    workloads = {}
+    if not args.no_skew and args.nbits == 28:
+        qf.close()
+        del keys, absent, present, out
+        torch.cuda.empty_cache()
+        workloads["skewed_counting"] = run_skew(args, torch, cqf_gb300)
+
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -367,6 +375,7 @@ def run_gpu(args, wl, rank, world):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "ref_cuda": ref_cuda,
+        "workloads": workloads,
         "clocks": clk,
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches // args.steps),
@@ -511,6 +520,94 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
         "what": "reference src/gqf.cu kernels compiled for sm_103a from its sources; host orchestration "
                 "restated (oracle/refgpu.py), thrust::sort replaced by torch.sort",
     }
+
+
+# ------------------------------------------------- skewed counting (config 3)
+
+def _exact_check(qf, keys, mask, torch):
+    """bulk_get of every distinct key (mod 2^(nbits+8)) equals its exact
+    multiplicity in keys; returns (ok, distinct)."""
+    u, c = torch.unique(keys & mask, return_counts=True)
+    out = torch.empty_like(u)
+    qf.bulk_get(u, out)
+    torch.cuda.synchronize()
+    return bool(torch.equal(out, c.to(torch.int64))), int(u.numel())
+
+
+def _time_reps(fn, reps, torch):
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - a)
+    return min(ts), statistics.median(ts)
+
+
+def run_skew(args, torch, cqf_gb300):
+    """Config 3 at full size on a fresh 2^28-slot filter per run:
+    (i) 2^28 Zipf(1.5) draws over 2^24 splitmix64 keys (seed 3) through
+    bulk_insert_reduce; (ii) canonical 31-mers of 2^20 150-bp reads (seed 4,
+    1% substitutions, genome of 2^24 bases) through gqf_bulk_insert_kmers.
+    Timed end to end on the device (events) per call, after warm-up; the
+    reference's CUDA reduce path (oracle/refgpu.py) on the same multisets."""
+    from cqf_gb300 import synth
+
+    nbits = 28
+    mask = (1 << (nbits + 8)) - 1
+    res = {}
+    keys = synth.zipf_keys_dev(3, 1 << 28, 1 << 24)
+    reads = synth.dna_reads_dev(4, 1 << 20, 150, 1 << 24, 0.01)
+    kmers = torch.empty(reads.shape[0] * 120, dtype=torch.int64, device="cuda")
+    cqf_gb300.kmers_extract(reads, 31, kmers)
+    kmers = kmers[kmers != -1]
+    torch.cuda.synchronize()
+    reps = max(2, min(args.steps, 5))
+    with cqf_gb300.QF(nbits) as qf:
+        for name, run, n, units in (
+            ("zipf_reduce", lambda: qf.bulk_insert_reduce(keys), keys.numel(), "draws"),
+            ("kmers_31", lambda: qf.bulk_insert_kmers(reads, 31), kmers.numel(), "k-mers"),
+        ):
+            def once():
+                qf.reset()
+                run()
+            for _ in range(2):
+                once()
+            tmin, tmed = _time_reps(once, reps, torch)
+            qf.reset()
+            run()
+            ok, distinct = _exact_check(qf, keys if name == "zipf_reduce" else kmers, mask, torch)
+            res[name] = {"mkeys_s": round(n / tmed / 1e6, 1), "mkeys_s_best": round(n / tmin / 1e6, 1),
+                         "ms": round(tmed * 1e3, 3), "keys": n, "units": units, "distinct": distinct,
+                         "exact_counts_equal": ok, "status": qf.status()}
+    if not args.no_ref_cuda:
+        from oracle import refgpu
+
+        if refgpu.available():
+            scratch = torch.empty(keys.numel(), dtype=torch.int64, device="cuda")
+            for name, src in (("zipf_reduce", keys), ("kmers_31", kmers)):
+                r = refgpu.RefGPU(nbits)
+                try:
+                    n = src.numel()
+                    scratch[:n].copy_(src)
+                    torch.cuda.synchronize()
+                    a = time.perf_counter()
+                    r.bulk_insert_reduce(scratch, n)
+                    torch.cuda.synchronize()
+                    dt = time.perf_counter() - a
+                finally:
+                    r.close()
+                res[name]["ref_cuda_mkeys_s"] = round(n / dt / 1e6, 1)
+                res[name]["speedup_vs_ref_cuda"] = round(res[name]["mkeys_s"] / (n / dt / 1e6), 2)
+            res["ref_cuda_what"] = ("reference kernels (hash_all, set_buffers_*, insert_from_buffers_thrust) "
+                                    "with torch.sort + unique_consecutive for thrust sort + reduce_by_key; "
+                                    "the reference's k-mer step is host code, so its arm starts from the "
+                                    "extracted k-mers")
+            del scratch
+    del keys, reads, kmers
+    torch.cuda.empty_cache()
+    return res
 
 
 # --------------------------------------------------------------- CPU arms

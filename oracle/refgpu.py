@@ -12,6 +12,11 @@ the CUDA driver API:
                set_buffer_lens, insert_from_buffers_hashed even then odd
   bulk_delete  (src/gqf.cu:3316-3363): the same with delete_from_buffers_hashed
   bulk_get     (src/gqf.cu:3397-3400): bulk_get_kernel, 512 threads per CTA
+  bulk_insert_reduce (src/gqf.cu:3238-3313): hash_all, sort, reduce_by_key,
+               set_buffers_binary / set_buffer_lens on the distinct hashes,
+               then insert_from_buffers_thrust (:2806) even then odd -- the
+               counted insert the reference function stops short of (it
+               returns after set_buffer_lens without launching an insert)
 
 thrust::sort is replaced by torch.sort (a device radix sort as well).  Like
 the reference, insert and delete overwrite the key buffer with sorted hashes.
@@ -38,7 +43,9 @@ KERNELS = {
     "insert_hashed": "_Z26insert_from_buffers_hashedP15quotient_filterm",
     "delete_hashed": "_Z26delete_from_buffers_hashedP15quotient_filterm",
     "bulk_get": "_Z15bulk_get_kernelP15quotient_filterPmmS1_h",
+    "insert_thrust": "_Z26insert_from_buffers_thrustP15quotient_filtermPmS1_",
 }
+CU_LIMIT_STACK_SIZE = 0x00
 
 
 def available() -> bool:
@@ -53,6 +60,7 @@ class _Driver:
         self.cu.cuLaunchKernel.argtypes = [ctypes.c_void_p] + [ctypes.c_uint] * 6 + [
             ctypes.c_uint, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p]
         self.cu.cuModuleUnload.argtypes = [ctypes.c_void_p]
+        self.cu.cuCtxSetLimit.argtypes = [ctypes.c_int, ctypes.c_size_t]
 
     def check(self, rc, what):
         if rc != 0:
@@ -73,6 +81,9 @@ class RefGPU:
         self.d = _Driver()
         with open(LAYOUT) as fh:
             self.lay = json.load(fh)
+        # per-thread stack of this process's context: the counted insert's
+        # frames (1120 bytes, all static) fit with a wide margin
+        self.d.check(self.d.cu.cuCtxSetLimit(CU_LIMIT_STACK_SIZE, 8192), "cuCtxSetLimit")
         self.mod = ctypes.c_void_p()
         self.d.check(self.d.cu.cuModuleLoad(ctypes.byref(self.mod), CUBIN.encode()), "cuModuleLoad")
         self.fn = {}
@@ -154,6 +165,28 @@ class RefGPU:
         qf, g = self._prelude(keys, n, flags)
         self._launch("insert_hashed", g, 32, qf, 0)
         self._launch("insert_hashed", g, 32, qf, 1)
+
+    def bulk_insert_reduce(self, keys, n=None, flags=0):
+        """keys: device int64 tensor, overwritten with sorted hashes."""
+        n = keys.numel() if n is None else n
+        if n == 0:
+            return
+        self.torch.cuda.synchronize()
+        qf = self.qf.data_ptr()
+        kp = keys.data_ptr()
+        self._launch("hash_all", (n - 1) // 32 + 1, 32, qf, kp, kp, n, (ctypes.c_uint8, flags))
+        s, _ = self.torch.sort(keys[:n])
+        keys[:n].copy_(s)
+        uk, cnt = self.torch.unique_consecutive(keys[:n], return_counts=True)  # reduce_by_key
+        uk = uk.contiguous()
+        cnt = cnt.to(self.torch.int64).contiguous()
+        u = uk.numel()
+        g = (self.num_locks - 1) // 32 + 1
+        self._launch("set_buffers_binary", g, 32, qf, u, uk.data_ptr(), (ctypes.c_uint8, flags))
+        self._launch("set_buffer_lens", g, 32, qf, u, uk.data_ptr())
+        self._launch("insert_thrust", g, 32, qf, 0, uk.data_ptr(), cnt.data_ptr())
+        self._launch("insert_thrust", g, 32, qf, 1, uk.data_ptr(), cnt.data_ptr())
+        self._hold = (uk, cnt)  # alive until the launches complete
 
     def bulk_delete(self, keys, n=None, flags=0):
         n = keys.numel() if n is None else n

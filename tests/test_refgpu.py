@@ -46,3 +46,25 @@ def test_reference_cuda_build_matches_oracle(refgpu, nbits):
         assert np.array_equal(a, b), first_diff(a, b)
     finally:
         r.close()
+
+
+@pytest.mark.parametrize("nbits", [12, 16])
+def test_reference_cuda_reduce_matches_oracle_and_product(refgpu, nbits):
+    import cqf_gb300
+    from cqf_gb300 import build, synth
+
+    keys = synth.zipf_keys(3, 1 << (nbits + 1), 1 << (nbits - 4))
+    r = refgpu.RefGPU(nbits)
+    o = oracle.Oracle(nbits)
+    try:
+        r.bulk_insert_reduce(dev(keys))
+        o.bulk_insert_reduce(keys)
+        a, b = o.dump(), r.dump()
+        assert np.array_equal(a, b), first_diff(a, b)
+    finally:
+        r.close()
+    build.build()
+    with cqf_gb300.QF(nbits) as qf:
+        qf.bulk_insert_reduce(dev(keys))
+        c = qf.export()
+        assert np.array_equal(a, c), first_diff(a, c)
