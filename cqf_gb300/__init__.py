@@ -59,6 +59,14 @@ SIGNATURES = {
     "gqf_bulk_insert_noalloc": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_insert_kmers": (_int, [_vp, _vp, _u64, _u32, _u32, _vp]),
     "gqf_kmers_extract": (_int, [_vp, _u64, _u32, _u32, _vp, _vp]),
+    "gqf_server_create": (_int, [_vp, _u64, ctypes.POINTER(_vp)]),
+    "gqf_server_submit": (ctypes.c_int64, [_vp, _int, _vp, _u64, _vp, _u32]),
+    "gqf_server_poll": (_int, [_vp, ctypes.c_int64]),
+    "gqf_server_wait": (_int, [_vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]),
+    "gqf_server_drain": (_int, [_vp]),
+    "gqf_server_stats": (_int, [_vp, _vp, _int]),
+    "gqf_server_reset_stats": (_int, [_vp]),
+    "gqf_server_destroy": (None, [_vp]),
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
@@ -292,6 +300,87 @@ class QF:
     def _ok(self, rc: int):
         if rc != 0:
             raise RuntimeError(last_error())
+
+
+OP_GET, OP_INSERT, OP_DELETE, OP_INSERT_REDUCE = 0, 1, 2, 3
+SERVE_DEVICE_PTRS = 1 << 8
+
+
+class Server:
+    """Serving loop over one resident filter (gqf_server_* in include/gqf.h).
+
+    submit() takes host arrays (numpy uint64, ideally in pinned memory such
+    as a pinned torch tensor) or device tensors; buffers must stay alive
+    until the request completes."""
+
+    STATS = ("requests", "launches", "keys", "p50_ms", "p99_ms", "max_ms", "staging_bytes", "peak_staging_bytes")
+
+    def __init__(self, qf: "QF", staging_bytes: int = 0):
+        self.L = load()
+        self.qf = qf
+        h = _vp()
+        if self.L.gqf_server_create(qf.h, staging_bytes, ctypes.byref(h)) != 0:
+            raise RuntimeError("gqf_server_create failed: " + last_error())
+        self.h = h
+
+    @staticmethod
+    def _buf(x):
+        if x is None:
+            return 0, False
+        if isinstance(x, np.ndarray):
+            return x.ctypes.data, False
+        if hasattr(x, "data_ptr"):
+            return x.data_ptr(), bool(getattr(x, "is_cuda", False))
+        return int(x), False
+
+    def submit(self, op: int, keys, counts=None, n: int | None = None, flags: int = 0) -> int:
+        kp, kdev = self._buf(keys)
+        cp, cdev = self._buf(counts)
+        if counts is not None and cdev != kdev:
+            raise ValueError("keys and counts must both be host or both be device buffers")
+        n = (keys.size if isinstance(keys, np.ndarray) else keys.numel()) if n is None else n
+        t = self.L.gqf_server_submit(self.h, op, kp, n, cp, flags | (SERVE_DEVICE_PTRS if kdev else 0))
+        if t < 0:
+            raise RuntimeError("gqf_server_submit failed: " + last_error())
+        return int(t)
+
+    def poll(self, ticket: int) -> int:
+        return int(self.L.gqf_server_poll(self.h, ticket))
+
+    def wait(self, ticket: int) -> float:
+        lat = ctypes.c_double(0)
+        if self.L.gqf_server_wait(self.h, ticket, ctypes.byref(lat)) != 0:
+            raise RuntimeError("request failed: " + last_error())
+        return lat.value
+
+    def drain(self):
+        if self.L.gqf_server_drain(self.h) != 0:
+            raise RuntimeError("server error: " + last_error())
+
+    def stats(self) -> dict:
+        out = np.zeros(len(self.STATS), dtype=np.float64)
+        self.L.gqf_server_stats(self.h, out.ctypes.data, out.size)
+        return {k: float(v) for k, v in zip(self.STATS, out)}
+
+    def reset_stats(self):
+        self.L.gqf_server_reset_stats(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gqf_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def kmers_extract(reads, k: int, out, stream=None):

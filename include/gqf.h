@@ -154,6 +154,46 @@ int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* r
 #define GQF_NOALLOC_SCRATCH_BYTES (16u << 20)
 int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
 
+/* ------------------------------------------------------------ serving loop
+ * No counterpart in the reference (its bulk calls run one at a time on the
+ * caller's device buffers).  A server keeps one filter resident and runs
+ * requests submitted from any host thread through a staging ring of
+ * staging_bytes in device memory (0 = a quarter of the free memory, at most
+ * 4 GiB): requests are admitted in arrival order as ring space frees up,
+ * consecutive requests of one kind (gets; inserts and counted inserts;
+ * deletes; QF_KEY_IS_HASH batches apart) run as one launch, and the copies of
+ * later launches overlap the compute of earlier ones.  Every request's result
+ * equals running the requests one by one in submission order.
+ *
+ * gqf_server_submit: op is GQF_OP_*; keys (and, for a get, counts: n
+ *   uint64 results) are host pointers -- pinned memory lets the copies run
+ *   asynchronously -- or device pointers with GQF_SERVE_DEVICE_PTRS in
+ *   flags; QF_KEY_IS_HASH may be or-ed in.  Buffers must stay valid until the
+ *   request completes.  Returns a ticket >= 0, or -1.
+ * gqf_server_poll: 1 done, 0 pending, -1 failed / unknown ticket.
+ * gqf_server_wait: blocks until done, frees the ticket, and stores the
+ *   request's latency (submission to completion, ms); 0 or -1.
+ * gqf_server_drain: waits until nothing is queued or in flight.
+ * gqf_server_stats: out[0..7] = requests completed, launches, keys, p50 ms,
+ *   p99 ms, max ms, staging bytes, peak staging bytes in use.
+ * While a server runs, other calls on its filter must not overlap it. */
+typedef struct gqf_server gqf_server;
+#define GQF_OP_GET 0
+#define GQF_OP_INSERT 1
+#define GQF_OP_DELETE 2
+#define GQF_OP_INSERT_REDUCE 3
+#define GQF_SERVE_DEVICE_PTRS (1u << 8)
+#define GQF_SERVE_STATS 8
+int gqf_server_create(QF* qf, uint64_t staging_bytes, gqf_server** out);
+int64_t gqf_server_submit(gqf_server* s, int op, const uint64_t* keys, uint64_t n, uint64_t* counts,
+                          uint32_t flags);
+int gqf_server_poll(gqf_server* s, int64_t ticket);
+int gqf_server_wait(gqf_server* s, int64_t ticket, double* latency_ms);
+int gqf_server_drain(gqf_server* s);
+int gqf_server_stats(gqf_server* s, double* out, int n);
+int gqf_server_reset_stats(gqf_server* s);
+void gqf_server_destroy(gqf_server* s);
+
 /* The filter's default stream for the reference entry points. */
 int gqf_set_stream(QF* qf, void* stream);
 
