@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-skew", action="store_true", help="skip the skewed-counting workloads")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop workload")
+    ap.add_argument("--serve-nbits", type=int, default=30)
+    ap.add_argument("--serve-load", type=float, default=0.7,
+                    help="Poisson offered load as a fraction of the measured saturated throughput")
     return ap.parse_args()
 
 
@@ -352,6 +356,10 @@ def run_gpu(args, wl, rank, world):
         del keys, absent, present, out
         torch.cuda.empty_cache()
         workloads["skewed_counting"] = run_skew(args, torch, cqf_gb300)
+    if not args.no_serve and rank == 0 and world == 1:
+        qf.close()
+        torch.cuda.empty_cache()
+        workloads["serving"] = run_serving(args, torch, cqf_gb300)
 
     line = {
         "metric": METRIC,
@@ -608,6 +616,215 @@ def run_skew(args, torch, cqf_gb300):
     del keys, reads, kmers
     torch.cuda.empty_cache()
     return res
+
+
+# ------------------------------------------------------ serving loop (config 5)
+
+def _u53(x):
+    return (x >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+
+
+class ServeStream:
+    """The request stream of the serving workload, from splitmix64 seed 11:
+    per request u0 -> exponential inter-arrival (unit mean, scaled by the
+    rate later), u1 -> op (50% get, 40% insert, 10% delete), u2 -> size
+    2^(10 + 14 u2) keys (log-uniform in [2^10, 2^24]).  Inserts take fresh
+    keys of one splitmix64 stream (seed 12) in order, deletes remove the
+    oldest inserted keys, gets ask for the n keys of that stream around the
+    insert cursor: up to n/2 already inserted (present unless deleted) and
+    the rest not yet inserted (absent when the get runs).  The stream ends
+    when inserted minus deleted keys reach 90% of the slots."""
+
+    def __init__(self, nbits):
+        from cqf_gb300 import synth
+
+        self.nslots = 1 << nbits
+        target = int(0.9 * self.nslots)
+        reqs, ins, dele, i = [], 0, 0, 0
+        chunk = 4096
+        while ins - dele < target:
+            u = _u53(synth.splitmix64(11, 3 * (i + chunk)))[3 * i:].reshape(-1, 3)
+            for u0, u1, u2 in u:
+                n = int(2 ** (10 + 14 * u2))
+                gap = -np.log(max(u0, 1e-300))
+                if u1 < 0.5:
+                    reqs.append(("get", n, gap, (ins, dele)))
+                elif u1 < 0.9:
+                    n = min(n, target - (ins - dele))
+                    reqs.append(("insert", n, gap, ins))
+                    ins += n
+                else:
+                    n = min(n, ins - dele)
+                    if n == 0:
+                        continue
+                    reqs.append(("delete", n, gap, dele))
+                    dele += n
+                if ins - dele >= target:
+                    break
+            i += chunk
+        self.reqs = reqs
+        self.n_insert = ins
+        self.total_keys = sum(r[1] for r in reqs)
+        self.mean_size = self.total_keys / len(reqs)
+
+
+def run_serving(args, torch, cqf_gb300):
+    """Config 5: one resident 2^30-slot filter served through gqf_server_*
+    from pinned host buffers.  (1) saturated: the whole stream submitted at
+    once -> sustained Mkeys/s; (2) Poisson arrivals at --serve-load of that
+    rate, submitted in real time -> p50/p99 latency (submission to results
+    on the host).  The reference arm runs the same stream one request at a
+    time (copy in, call, copy out): its latencies follow from its measured
+    service times, FIFO, with the same arrival times."""
+    import queue
+
+    from cqf_gb300 import synth
+
+    nbits = args.serve_nbits
+    st = ServeStream(nbits)
+    npool = st.n_insert + (1 << 24)
+    pool = torch.empty(npool, dtype=torch.int64, pin_memory=True)
+    for a in range(0, npool, 1 << 26):
+        b = min(npool, a + (1 << 26))
+        pool[a:b].copy_(synth._splitmix_range_dev(12, a, b, "cuda"))
+    out_cap = 1 << 28
+    outbuf = torch.empty(out_cap, dtype=torch.int64, pin_memory=True)
+    torch.cuda.synchronize()
+
+    def payload(r):
+        """(keys, present range within them) of a request."""
+        kind, n, _, arg = r
+        if kind != "get":
+            return pool[arg:arg + n], None
+        ins, dele = arg
+        s0 = max(0, ins - n // 2)
+        return pool[s0:s0 + n], (max(dele, s0) - s0, ins - s0)
+
+    def run(realtime_rate=None):
+        qf = cqf_gb300.QF(nbits)
+        srv = cqf_gb300.Server(qf)
+        ops = {"get": cqf_gb300.OP_GET, "insert": cqf_gb300.OP_INSERT, "delete": cqf_gb300.OP_DELETE}
+        q = queue.Queue()
+        checks = {"ok": True, "checked": 0}
+        lat = []
+        prog = {"done": -1}
+
+        def waiter():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                seq, t, out, pr = item
+                lat.append(srv.wait(t))
+                if out is not None:  # the inserted, undeleted keys are found
+                    a, b = pr
+                    b = min(b, a + 4096)
+                    checks["ok"] &= bool((out[a:b] > 0).all())
+                    checks["checked"] += 1
+                prog["done"] = seq
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        users = []  # (seq, start, end) of output slices still to be checked
+        oat = 0
+        t0 = time.perf_counter()
+        sched = 0.0
+        lag = 0.0
+        for seq, r in enumerate(st.reqs):
+            kind, n = r[0], r[1]
+            if realtime_rate:
+                sched += r[2] / realtime_rate
+                now = time.perf_counter() - t0
+                if sched > now:
+                    time.sleep(sched - now)
+                lag = max(lag, time.perf_counter() - t0 - sched)
+            keys, pr = payload(r)
+            out = None
+            if kind == "get":
+                if oat + n > out_cap:
+                    oat = 0
+                a, b = oat, oat + n
+                oat = b
+                # reuse an output slice only after its previous request was checked
+                while any(sq > prog["done"] and u0 < b and a < u1 for sq, u0, u1 in users):
+                    time.sleep(50e-6)
+                users = [u for u in users if u[0] > prog["done"]] + [(seq, a, b)]
+                out = outbuf[a:b].numpy()
+            t = srv.submit(ops[kind], keys, out)
+            q.put((seq, t, out, pr))
+        q.put(None)
+        th.join()
+        srv.drain()
+        dt = time.perf_counter() - t0
+        stats = srv.stats()
+        srv.close()
+        qf.close()
+        lat_sorted = np.sort(np.array(lat))
+        return {"seconds": dt, "mkeys_s": st.total_keys / dt / 1e6,
+                "p50_ms": float(np.percentile(lat_sorted, 50)), "p99_ms": float(np.percentile(lat_sorted, 99)),
+                "max_ms": float(lat_sorted[-1]), "launches": int(stats["launches"]),
+                "peak_staging_gb": stats["peak_staging_bytes"] / 1e9, "staging_gb": stats["staging_bytes"] / 1e9,
+                "submit_lag_max_ms": lag * 1e3, "present_found": checks["ok"],
+                "gets_checked": checks["checked"]}
+
+    sat = run(None)
+    rate = args.serve_load * sat["mkeys_s"] * 1e6 / st.mean_size  # requests per second
+    pois = run(rate)
+    rnd = lambda d: {k: round(v, 3) if isinstance(v, float) else v for k, v in d.items()}
+    res = {
+        "requests": len(st.reqs),
+        "keys": st.total_keys,
+        "mix": {k: sum(1 for r in st.reqs if r[0] == k) for k in ("get", "insert", "delete")},
+        "nbits": nbits,
+        "saturated": rnd(sat),
+        "poisson": rnd(pois) | {"rate_req_s": round(rate, 1), "offered_mkeys_s": round(rate * st.mean_size / 1e6, 1)},
+        "what": "gqf_server from pinned host buffers; latency = submission to results on the host",
+    }
+    if not args.no_ref_cuda:
+        res["ref_cuda"] = run_serving_ref(st, nbits, pool, rate, torch)
+        if "poisson_p99_ms" in res["ref_cuda"]:
+            res["p99_ref_cuda_over_ours"] = round(res["ref_cuda"]["poisson_p99_ms"] / max(1e-9, pois["p99_ms"]), 2)
+    del pool, outbuf
+    return res
+
+
+def run_serving_ref(st, nbits, pool, rate, torch):
+    from oracle import refgpu
+
+    if not refgpu.available():
+        return {"unavailable": "reference cubin not built"}
+    r = refgpu.RefGPU(nbits)
+    dbuf = torch.empty(1 << 24, dtype=torch.int64, device="cuda")
+    dout = torch.empty(1 << 24, dtype=torch.int64, device="cuda")
+    hout = torch.empty(1 << 24, dtype=torch.int64, pin_memory=True)
+    service = []
+    try:
+        for kind, n, _, arg in st.reqs:
+            s0 = arg if kind != "get" else max(0, arg[0] - n // 2)
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            dbuf[:n].copy_(pool[s0:s0 + n], non_blocking=True)
+            if kind == "get":
+                r.bulk_get(dbuf, dout, n)
+                hout[:n].copy_(dout[:n], non_blocking=True)
+            else:
+                (r.bulk_insert if kind == "insert" else r.bulk_delete)(dbuf, n)
+            torch.cuda.synchronize()
+            service.append(time.perf_counter() - a)
+    finally:
+        r.close()
+    arrivals = np.cumsum([q[2] for q in st.reqs]) / rate
+    done, lat = 0.0, []
+    for arr, sv in zip(arrivals, service):
+        done = max(done, arr) + sv
+        lat.append(done - arr)
+    lat = np.array(lat) * 1e3
+    busy = sum(service)
+    return {"busy_seconds": round(busy, 3), "mkeys_s": round(st.total_keys / busy / 1e6, 1),
+            "poisson_p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "poisson_p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "what": "reference CUDA build, one request at a time (copy in, bulk call, copy out); "
+                    "FIFO latencies from measured service times at the same arrival times"}
 
 
 # --------------------------------------------------------------- CPU arms

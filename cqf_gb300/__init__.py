@@ -70,6 +70,8 @@ SIGNATURES = {
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
+    "gqf_set_sparse_max": (_int, [_vp, _u32]),
+    "gqf_get_sparse_max": (ctypes.c_int64, [_vp]),
     "gqf_nslots": (_u64, [_vp]),
     "gqf_xnslots": (_u64, [_vp]),
     "gqf_nblocks": (_u64, [_vp]),
@@ -183,6 +185,12 @@ class QF:
     def set_region_log(self, lr: int):
         if self.L.gqf_set_region_log(self.h, int(lr)) != 0:
             raise ValueError(last_error())
+
+    def set_sparse_max(self, n: int):
+        self._ok(self.L.gqf_set_sparse_max(self.h, n))
+
+    def sparse_max(self) -> int:
+        return int(self.L.gqf_get_sparse_max(self.h))
 
     def region_log(self) -> int:
         return int(self.L.gqf_get_region_log(self.h))

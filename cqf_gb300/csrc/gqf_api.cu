@@ -45,6 +45,7 @@ struct HostFilter {
   cudaStream_t stream = 0;  // legacy default stream, like the reference
   int log_region = 12;
   bool auto_region = true;
+  uint32_t sparse_max = kDefaultSparseMax;  // regions with <= this many keys go key by key
   uint8_t* aux = nullptr;   // status word + miss counter
   Partition part{};
   uint64_t key_cap = 0;
@@ -217,7 +218,8 @@ int do_bulk_reduce(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flag
   }
   {
     PhaseTimer t(f, GQF_PROF_INSERT, st, n);
-    if (!ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st), "rebuild")) return -1;
+    if (!ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st, f->sparse_max), "rebuild"))
+      return -1;
   }
   return 0;
 }
@@ -239,7 +241,7 @@ int do_bulk(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, Op o
   }
   {
     PhaseTimer t(f, op == Op::kDelete ? GQF_PROF_DELETE : GQF_PROF_INSERT, st, n);
-    if (!ck(launch_rebuild(f->g, p, op, f->dqf, status_ptr(f), st), "rebuild")) return -1;
+    if (!ck(launch_rebuild(f->g, p, op, f->dqf, status_ptr(f), st, f->sparse_max), "rebuild")) return -1;
   }
   return 0;
 }
@@ -498,6 +500,19 @@ int gqf_set_region_log(QF* qf, int log_region) {
   f->auto_region = false;
   f->log_region = log_region;
   return 0;
+}
+
+int gqf_set_sparse_max(QF* qf, uint32_t max_keys) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(f->mu);
+  f->sparse_max = max_keys;
+  return 0;
+}
+
+int64_t gqf_get_sparse_max(QF* qf) {
+  HostFilter* f = lookup(qf);
+  return f ? (int64_t)f->sparse_max : -1;
 }
 
 int gqf_get_region_log(QF* qf) {

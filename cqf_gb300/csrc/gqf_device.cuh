@@ -295,6 +295,35 @@ struct Serial {
     }
   }
 
+  // Window check of a key-by-key update (not in the reference): applying
+  // changes that add at most `grow` slots (0 for removals) to the runs of
+  // quotients below region_end touches nothing at or past `bound` if the
+  // max(grow, 1)-th empty slot after T, the end of those runs, lies below
+  // `bound`.  Every change happens at or before T, or moves slots up to the
+  // first empty slot after the change, and each added slot consumes one
+  // empty slot; a removal only moves slots down inside its cluster, which
+  // ends at the first empty slot after it.  region_end is a block boundary
+  // below nslots.
+  GQF_HDF bool sparse_fits(uint64_t region_end, uint64_t grow, uint64_t bound) const {
+    uint64_t x = region_end + b[region_end / 64].offset;  // T + 1
+    const uint64_t need = grow ? grow : 1;
+    for (uint64_t j = 0; j < need; j++) {
+      if (x >= bound) return false;
+      x = find_first_empty_slot(x);
+      if (x >= bound) return false;
+      x++;
+    }
+    return true;
+  }
+
+  // Upper bound on the slots an insert of `count` copies of one hash adds.
+  GQF_HDF static uint64_t insert_growth(uint64_t count) {
+    if (count <= 1) return 1;
+    uint8_t enc[16];
+    int a = encode_counter(0, count, enc), c = encode_counter(1, count, enc);
+    return (uint64_t)(a > c ? a : c) + 1;
+  }
+
   // insert_replace_slots_and_shift_remainders_and_runends_and_offsets
   // (src/gqf.cu:1013-1097).  Offsets are exact, so they add without
   // saturating.

@@ -94,9 +94,11 @@ cudaError_t launch_kmers(const uint8_t* reads, uint64_t nreads, uint32_t read_le
                          cudaStream_t st);
 
 // Even regions, then odd regions, then the serial fallback for regions whose
-// rebuild window was exceeded.
+// rebuild window was exceeded.  Regions holding at most sparse_max keys are
+// updated key by key instead of rebuilt (0: rebuild every region).
+constexpr uint32_t kDefaultSparseMax = 32;
 cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_filter* dqf,
-                           uint32_t* status, cudaStream_t st);
+                           uint32_t* status, cudaStream_t st, uint32_t sparse_max = kDefaultSparseMax);
 size_t rebuild_smem_bytes(int log_region);
 
 cudaError_t launch_export(const Geom& g, uint8_t* packed, cudaStream_t st);

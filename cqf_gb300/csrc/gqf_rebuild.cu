@@ -209,6 +209,7 @@ __device__ int scan_sum(int v, int* tmp, int* total) {
 // the duplicate-merging pass of bulk_insert_reduce.
 template <int LOGS, bool DEL, bool CNT>
 __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom g, Partition p, int parity,
+                                                                             uint32_t sparse_max,
                                                                              uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom
   const uint32_t r = 2 * blockIdx.x + parity;
   if (r >= p.nregions) return;
   const uint32_t kbeg = p.region_start[r], kend = kbeg + p.region_count[r];
-  if (kbeg == kend) return;
+  if (kend - kbeg <= sparse_max) return;  // empty, or taken by k_sparse
   const int tid = threadIdx.x;
 
   const uint64_t base = (uint64_t)r << LOGS;
@@ -581,6 +582,53 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom
   }
 }
 
+// Sparse regions.  The rebuild visits every quotient and slot of its window
+// whatever the number of keys, so a region holding only a few keys (a small
+// batch, or a large table) is cheaper to update key by key: one thread per
+// region applies the reference's single-key algorithms (gqf_device.cuh,
+// src/gqf.cu:1523 insert1, :1768 insert, :1876 _remove) in place, as the
+// reference's insert_from_buffers_hashed does for every region
+// (src/gqf.cu:2759-2804).
+//
+// Before writing anything the thread proves (Serial::sparse_fits) that the
+// region's changes stay inside the window a rebuild would own, [base, base +
+// REG + PUSH); otherwise the region is deferred untouched to the serial
+// fallback.
+template <int LOGS, bool DEL, bool CNT>
+__global__ void __launch_bounds__(128) k_sparse(const quotient_filter* dqf, Partition p, int parity,
+                                                uint32_t sparse_max, uint32_t* status) {
+  const uint32_t r = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + parity;
+  if (r >= p.nregions) return;
+  const uint32_t cnt = p.region_count[r];
+  if (cnt == 0 || cnt > sparse_max) return;
+  const Serial S(dqf);
+  const uint32_t kbeg = p.region_start[r];
+  const uint64_t base = (uint64_t)r << LOGS;
+  const uint64_t region_end = base + (1ULL << LOGS);  // a block boundary below nslots
+  const uint64_t bound = min(base + (uint64_t)Lay<LOGS, false>::WIN, min(S.xnslots, 64 * S.nblocks));
+  uint64_t grow = 0;  // slots the batch may add (0 for deletes)
+  if (!DEL)
+    for (uint32_t k = kbeg; k < kbeg + cnt; k++) grow += Serial::insert_growth(CNT ? p.counts[k] : 1);
+  if (!S.sparse_fits(region_end, grow, bound)) {
+    const uint32_t at = atomicAdd(&p.deferred[0], 1u);
+    p.deferred[1 + at] = r;
+    atomicOr(status, kStDeferred);
+    if (p.stats) atomicAdd(&p.stats[0], 1ULL);
+    return;
+  }
+  const int shift = 8 + LOGS;
+  for (uint32_t k = kbeg; k < kbeg + cnt; k++) {
+    const uint64_t h = ((uint64_t)r << shift) | p.keys[k];
+    if (DEL) {
+      S.remove(h, 1);
+    } else {
+      const uint64_t c = CNT ? p.counts[k] : 1;
+      const int rc = c == 1 ? S.insert1(h) : S.insert(h, c);
+      if (rc < 0) atomicOr(status, kStFull);
+    }
+  }
+}
+
 // Serial fallback for deferred regions: the reference's single-key
 // operations, one key at a time, in region order.
 __global__ void k_fallback(quotient_filter* dqf, Partition p, int del, uint32_t* status) {
@@ -624,7 +672,8 @@ void configure() {
 }
 
 template <int LOGS>
-cudaError_t run_phases(const Geom& g, const Partition& p, Op op, uint32_t* status, cudaStream_t st) {
+cudaError_t run_phases(const Geom& g, const Partition& p, Op op, const quotient_filter* dqf, uint32_t sparse_max,
+                       uint32_t* status, cudaStream_t st) {
   const bool cnt = p.counts != nullptr;
   if (op == Op::kDelete && cnt) return cudaErrorInvalidValue;  // deletes carry no counts
   if (op == Op::kDelete) configure<LOGS, true, false>();
@@ -634,12 +683,22 @@ cudaError_t run_phases(const Geom& g, const Partition& p, Op op, uint32_t* statu
   for (int parity = 0; parity < 2; parity++) {
     uint32_t grid = parity ? p.nregions / 2 : half;
     if (!grid) continue;
+    if (sparse_max) {
+      const uint32_t sg = (grid + 127) / 128;
+      if (op == Op::kDelete)
+        k_sparse<LOGS, true, false><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
+      else if (cnt)
+        k_sparse<LOGS, false, true><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
+      else
+        k_sparse<LOGS, false, false><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
+      count_launch();
+    }
     if (op == Op::kDelete)
-      k_rebuild<LOGS, true, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, status);
+      k_rebuild<LOGS, true, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, sparse_max, status);
     else if (cnt)
-      k_rebuild<LOGS, false, true><<<grid, 256, Lay<LOGS, true>::BYTES, st>>>(g, p, parity, status);
+      k_rebuild<LOGS, false, true><<<grid, 256, Lay<LOGS, true>::BYTES, st>>>(g, p, parity, sparse_max, status);
     else
-      k_rebuild<LOGS, false, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, status);
+      k_rebuild<LOGS, false, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, sparse_max, status);
     count_launch();
   }
   return cudaGetLastError();
@@ -657,13 +716,13 @@ size_t rebuild_smem_bytes(int log_region) {
 }
 
 cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_filter* dqf,
-                           uint32_t* status, cudaStream_t st) {
+                           uint32_t* status, cudaStream_t st, uint32_t sparse_max) {
   cudaError_t e = cudaMemsetAsync(p.deferred, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   switch (p.log_region) {
-    case 11: e = run_phases<11>(g, p, op, status, st); break;
-    case 12: e = run_phases<12>(g, p, op, status, st); break;
-    case 13: e = run_phases<13>(g, p, op, status, st); break;
+    case 11: e = run_phases<11>(g, p, op, dqf, sparse_max, status, st); break;
+    case 12: e = run_phases<12>(g, p, op, dqf, sparse_max, status, st); break;
+    case 13: e = run_phases<13>(g, p, op, dqf, sparse_max, status, st); break;
     default: return cudaErrorInvalidValue;
   }
   if (e != cudaSuccess) return e;

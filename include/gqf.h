@@ -202,6 +202,13 @@ int gqf_set_stream(QF* qf, void* stream);
 int gqf_set_region_log(QF* qf, int log_region);
 int gqf_get_region_log(QF* qf);
 
+/* Regions that receive at most max_keys keys of a batch are updated key by
+ * key (the reference's single-key algorithms, one thread per region) instead
+ * of rebuilt; 0 rebuilds every touched region.  Does not change results, only
+ * speed.  Default 32. */
+int gqf_set_sparse_max(QF* qf, uint32_t max_keys);
+int64_t gqf_get_sparse_max(QF* qf);
+
 /* Geometry: 2^nbits slots, xnslots = nslots + 10 sqrt(nslots) slots in
  * 64-slot blocks (qf_init, src/gqf.cu:1939-1996). */
 uint64_t gqf_nslots(QF* qf);

@@ -357,3 +357,85 @@ def exact_counts(keys: np.ndarray, nbits: int, probe: np.ndarray) -> np.ndarray:
     i = np.minimum(i, max(0, u.size - 1))
     hit = (u.size > 0) & (u[i] == p) if u.size else np.zeros(p.shape, dtype=bool)
     return np.where(hit, cnt[i] if u.size else 0, 0).astype(np.uint64)
+
+
+def encode_counter(rem: int, count: int) -> list:
+    """Slots of one counter (src/gqf.cu:1216-1273), first slot first: count 1
+    is [rem], 2 is [rem, rem], 3 is [rem, 0, rem]; larger counts store
+    count - 3 (count - 4 for remainder 0) in base 254 (255) digits between
+    two copies of rem, digits shifted past rem, a 0 escape when the leading
+    digit is not below rem, and a trailing 0 for remainder 0."""
+    if count == 0:
+        return []
+    if count == 1:
+        return [rem]
+    if count == 2:
+        return [rem, rem]
+    if count == 3:
+        return [rem, 0, rem]
+    base = 254 if rem else 255
+    c = count - (3 if rem else 4)
+    digits = []
+    while True:
+        d = c % base + 1
+        if rem and d >= rem:
+            d += 1
+        digits.append(d)
+        c //= base
+        if not c:
+            break
+    out = [rem]
+    if rem and digits[-1] >= rem:
+        out.append(0)
+    out += digits[::-1]
+    if rem == 0:
+        out.append(0)
+    out.append(rem)
+    return out
+
+
+def canonical_dump(nbits: int, counts: dict) -> np.ndarray:
+    """The packed filter (120-byte metadata + 81-byte blocks) that any history
+    leaving the multiset `counts` (hash -> count) produces in the reference's
+    insert path: runs in quotient order, counters in remainder order, each run
+    at max(quotient, end of the previous run + 1), offsets min(255, exact).
+    The metadata is taken from an empty oracle filter.  Raises if the runs
+    do not fit the table."""
+    o = Oracle(nbits)
+    meta = o.dump()[:120].copy()
+    nblocks, xn = o.nblocks, o.xnslots
+    o.close()
+    slots = np.zeros(64 * nblocks, dtype=np.uint8)
+    occ = np.zeros(64 * nblocks, dtype=np.uint8)
+    run = np.zeros(64 * nblocks, dtype=np.uint8)
+    by_q = {}
+    for h, c in counts.items():
+        if c:
+            by_q.setdefault(int(h) >> 8, []).append((int(h) & 255, int(c)))
+    end = -1
+    ends = {}
+    for q in sorted(by_q):
+        s = max(q, end + 1)
+        body = []
+        for rem, c in sorted(by_q[q]):
+            body += encode_counter(rem, c)
+        if s + len(body) > xn:
+            raise ValueError("multiset does not fit the table")
+        slots[s:s + len(body)] = body
+        end = s + len(body) - 1
+        occ[q] = 1
+        run[end] = 1
+        ends[q] = end
+    offs = np.zeros(nblocks, dtype=np.int64)
+    qs = np.array(sorted(ends), dtype=np.int64)
+    es = np.array([ends[q] for q in qs], dtype=np.int64)
+    for b in range(1, nblocks):
+        k = np.searchsorted(qs, 64 * b) - 1
+        if k >= 0:
+            offs[b] = max(0, int(es[k]) - 64 * b + 1)
+    blk = np.zeros((nblocks, 81), dtype=np.uint8)
+    blk[:, 0] = np.minimum(255, offs)
+    blk[:, 1:9] = np.packbits(occ.reshape(nblocks, 64), axis=1, bitorder="little")
+    blk[:, 9:17] = np.packbits(run.reshape(nblocks, 64), axis=1, bitorder="little")
+    blk[:, 17:] = slots.reshape(nblocks, 64)
+    return np.concatenate([meta, blk.reshape(-1)])

@@ -27,3 +27,29 @@ void sh_export(void* p, uint8_t* out) {
   }
 }
 }
+extern "C" {
+int sh_sparse_fits(void* p, uint64_t region_end, uint64_t grow, uint64_t bound) {
+  return Serial((quotient_filter*)p).sparse_fits(region_end, grow, bound) ? 1 : 0;
+}
+uint64_t sh_insert_growth(uint64_t count) { return Serial::insert_growth(count); }
+int64_t sh_snapshot(void* p, Block* out) {
+  quotient_filter* q = (quotient_filter*)p;
+  memcpy(out, q->blocks, q->nblocks * sizeof(Block));
+  return (int64_t)q->nblocks;
+}
+// Highest slot whose byte, occupied or runend bit differs from the snapshot
+// (a changed block offset counts as the block's first slot); -1 if none.
+int64_t sh_highest_change(void* p, const Block* before) {
+  quotient_filter* q = (quotient_filter*)p;
+  for (int64_t b = (int64_t)q->nblocks - 1; b >= 0; b--) {
+    const Block& x = q->blocks[b];
+    const Block& y = before[b];
+    for (int j = 63; j >= 0; j--)
+      if (x.slots[j] != y.slots[j] || (((x.runends ^ y.runends) >> j) & 1ULL) ||
+          (((x.occupieds ^ y.occupieds) >> j) & 1ULL))
+        return 64 * b + j;
+    if (x.offset != y.offset) return 64 * b;
+  }
+  return -1;
+}
+}

@@ -146,3 +146,32 @@ def test_oracle_matches_reference_live(seed):
         probe = oracle.splitmix64(seed + 1000, n)
         assert np.array_equal(r.bulk_get(probe), o.bulk_get(probe))
         r.close()
+
+
+@pytest.mark.parametrize("nbits", [8, 11])
+def test_canonical_dump_matches_oracle(nbits):
+    """oracle.canonical_dump (the layout as a function of the multiset) equals
+    the oracle after insert, counted-insert and delete histories that keep
+    every block offset below 255."""
+    from collections import Counter
+
+    rng = np.random.default_rng(nbits)
+    o = oracle.Oracle(nbits)
+    ms = Counter()
+    checked = 0
+    for step in range(12):
+        n = int(rng.integers(1, 1 << (nbits - 2)))
+        k = oracle.skewed_keys(int(rng.integers(1 << 30)), n, nbits - 2)
+        if step % 3 == 2:
+            o.bulk_delete(k)
+            for h in oracle.hash64(k, nbits).tolist():
+                ms[h] = max(0, ms[h] - 1)
+        else:
+            (o.bulk_insert_reduce if step % 3 else o.bulk_insert)(k)
+            ms.update(oracle.hash64(k, nbits).tolist())
+        d = o.dump()
+        if oracle.parse_dump(d)[1].max() < 255:
+            assert np.array_equal(d, oracle.canonical_dump(nbits, ms)), step
+            checked += 1
+    assert checked >= 4
+    assert oracle.encode_counter(7, 1) == [7] and oracle.encode_counter(0, 3) == [0, 0, 0]

@@ -34,6 +34,13 @@ def lib(tmp_path_factory):
     L.sh_count.restype = u64
     L.sh_count.argtypes = [vp, u64]
     L.sh_export.argtypes = [vp, vp]
+    L.sh_sparse_fits.argtypes = [vp, u64, u64, u64]
+    L.sh_insert_growth.restype = u64
+    L.sh_insert_growth.argtypes = [u64]
+    L.sh_snapshot.restype = ctypes.c_int64
+    L.sh_snapshot.argtypes = [vp, vp]
+    L.sh_highest_change.restype = ctypes.c_int64
+    L.sh_highest_change.argtypes = [vp, vp]
     return L
 
 
@@ -90,3 +97,71 @@ def test_walks_stop_at_the_table_end(lib):
         else:
             o.remove_hash(h, 1)
             lib.sh_remove(q, h)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_sparse_window_check_bounds_every_change(lib, seed):
+    """The key-by-key path's pre-check (Serial::sparse_fits): whenever it
+    accepts a region's batch, applying the batch changes nothing at or past
+    the bound.  Regions of 256 quotients with a 384-slot window, driven to
+    93% of the slots with counted inserts and deletes; the end state is the
+    canonical layout of the multiset."""
+    from collections import Counter
+
+    rng = np.random.default_rng(seed)
+    nbits, lr = 13, 8
+    reg = 1 << lr
+    o = oracle.Oracle(nbits)
+    q = lib.sh_new(nbits)
+    snap = np.zeros(o.nblocks * 96, dtype=np.uint8)
+    ms = Counter()
+    used = 0  # slots the multiset's counters take
+    live = []
+    accepted = rejected = 0
+
+    def slots(h, c):
+        return len(oracle.encode_counter(h & 255, c))
+
+    while used < int(0.93 * (1 << nbits)) and accepted + rejected < 6000:
+        r = int(rng.integers(0, (1 << nbits) >> lr))
+        k = int(rng.integers(1, 12))
+        delete = live and rng.random() < 0.25
+        if delete:
+            hs = [live[int(i)] for i in rng.integers(0, len(live), size=k)]
+            counts = [1] * k
+        else:
+            qs = rng.integers(r * reg, (r + 1) * reg, size=k).astype(np.uint64)
+            rs = rng.integers(0, 256, size=k).astype(np.uint64)
+            hs = [int(x) for x in (qs << np.uint64(8)) | rs]
+            counts = [int(rng.choice([1, 1, 1, 2, 3, 300, 70000])) for _ in hs]
+        rr = (hs[0] >> 8) >> lr
+        keep = [i for i, h in enumerate(hs) if ((h >> 8) >> lr) == rr]
+        hs, counts = [hs[i] for i in keep], [counts[i] for i in keep]
+        grow = 0 if delete else sum(int(lib.sh_insert_growth(c)) for c in counts)
+        bound = min(rr * reg + reg + reg // 2, o.xnslots)
+        fits = lib.sh_sparse_fits(q, (rr + 1) * reg, grow, bound)
+        lib.sh_snapshot(q, snap.ctypes.data)
+        for h, c in zip(hs, counts):
+            old = ms[h]
+            if delete:
+                lib.sh_remove(q, h)
+                ms[h] = max(0, old - 1)
+                if h in live:
+                    live.remove(h)
+            else:
+                lib.sh_insert(q, h, c) if c > 1 else lib.sh_insert1(q, h)
+                ms[h] = old + c
+                live.append(h)
+            used += slots(h, ms[h]) - slots(h, old)
+        hi = lib.sh_highest_change(q, snap.ctypes.data)
+        if fits:
+            accepted += 1
+            assert hi < bound, (hi, bound, grow, delete)
+        else:
+            rejected += 1
+    assert accepted > 500
+    # the canonical layout of the multiset (the oracle itself meets the
+    # reference's 8-bit offset defect on such long clusters)
+    b = np.zeros(o.nblocks * 81, dtype=np.uint8)
+    lib.sh_export(q, b.ctypes.data)
+    assert np.array_equal(oracle.canonical_dump(nbits, ms)[120:], b)
