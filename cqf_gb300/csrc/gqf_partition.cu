@@ -49,24 +49,21 @@ __global__ void __launch_bounds__(256) k_part_count(Geom g, const uint64_t* __re
   }
 }
 
-// Exclusive scan of nregions counts by one CTA; also resets the cursors.
-__global__ void __launch_bounds__(1024) k_part_scan(const uint32_t* __restrict__ region_count,
-                                                    uint32_t* __restrict__ region_start,
-                                                    uint32_t* __restrict__ cursor, uint32_t nregions) {
-  __shared__ uint32_t warp_sum[32];
-  const uint32_t per = (nregions + blockDim.x - 1) / blockDim.x;
-  const uint32_t a = threadIdx.x * per;
-  const uint32_t b = min(a + per, nregions);
-  uint32_t s = 0;
-  for (uint32_t i = a; i < b; i++) s += region_count[i];
-  // block exclusive scan of s
-  uint32_t v = s;
+// Exclusive scan of the nregions counts (also resetting the cursors), in
+// chunks of kScanChunk regions: one CTA per chunk sums it, then one CTA per
+// chunk adds the sums of the chunks before it and scans its own.  Loads and
+// stores are coalesced: thread t of a CTA owns counts 4t..4t+3 of the chunk.
+constexpr int kScanThreads = 1024;
+constexpr int kScanChunk = 4 * kScanThreads;
+
+__device__ __forceinline__ uint32_t block_sum_excl(uint32_t v, uint32_t* warp_sum, uint32_t* total) {
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= (unsigned)o) v += t;
+    uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (unsigned)o) x += t;
   }
-  if (lane == 31) warp_sum[wid] = v;
+  if (lane == 31) warp_sum[wid] = x;
   __syncthreads();
   if (wid == 0) {
     uint32_t w = lane < (blockDim.x >> 5) ? warp_sum[lane] : 0;
@@ -77,13 +74,54 @@ __global__ void __launch_bounds__(1024) k_part_scan(const uint32_t* __restrict__
     warp_sum[lane] = w;
   }
   __syncthreads();
-  uint32_t excl = v - s + (wid ? warp_sum[wid - 1] : 0);
-  for (uint32_t i = a; i < b; i++) {
-    region_start[i] = excl;
-    cursor[i] = excl;
-    excl += region_count[i];
+  const uint32_t r = x - v + (wid ? warp_sum[wid - 1] : 0);
+  *total = warp_sum[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ void load4(const uint32_t* a, uint32_t n, uint32_t i, uint32_t* v) {
+  for (int k = 0; k < 4; k++) v[k] = i + k < n ? a[i + k] : 0u;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(const uint32_t* __restrict__ region_count,
+                                                            uint32_t nregions, uint32_t* __restrict__ sums) {
+  __shared__ uint32_t warp_sum[32];
+  uint32_t v[4];
+  load4(region_count, nregions, blockIdx.x * kScanChunk + 4 * threadIdx.x, v);
+  uint32_t tot;
+  block_sum_excl(v[0] + v[1] + v[2] + v[3], warp_sum, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t* __restrict__ region_count,
+                                                             uint32_t nregions, const uint32_t* __restrict__ sums,
+                                                             uint32_t* __restrict__ region_start,
+                                                             uint32_t* __restrict__ cursor) {
+  __shared__ uint32_t warp_sum[32];
+  uint32_t before = 0, dummy;  // sum of the chunks before this one
+  for (uint32_t c = threadIdx.x; c < blockIdx.x; c += blockDim.x) before += sums[c];
+  {
+    uint32_t part = before;
+    for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = part;
+    __syncthreads();
+    before = 0;
+    for (unsigned w = 0; w < (blockDim.x >> 5); w++) before += warp_sum[w];
+    __syncthreads();
   }
-  if (threadIdx.x == blockDim.x - 1) region_start[nregions] = excl;
+  const uint32_t i = blockIdx.x * kScanChunk + 4 * threadIdx.x;
+  uint32_t v[4];
+  load4(region_count, nregions, i, v);
+  uint32_t excl = before + block_sum_excl(v[0] + v[1] + v[2] + v[3], warp_sum, &dummy);
+  for (int k = 0; k < 4; k++) {
+    if (i + k < nregions) {
+      region_start[i + k] = excl;
+      cursor[i + k] = excl;
+    }
+    excl += v[k];
+    if (i + k + 1 == nregions) region_start[nregions] = excl;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_part_scatter(Geom g, const uint64_t* __restrict__ keys,
@@ -146,8 +184,14 @@ cudaError_t launch_partition_counted(const Geom& g, const Partition& p, const ui
     k_part_count<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, key_is_hash, shift, p.region_count, status);
     count_launch();
   }
-  k_part_scan<<<1, 1024, 0, st>>>(p.region_count, p.region_start, p.cursor, p.nregions);
-  count_launch();
+  {
+    // the chunk sums use the deferred list as scratch: the rebuild resets it
+    const uint32_t chunks = (p.nregions + kScanChunk - 1) / kScanChunk;
+    k_scan_sums<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred);
+    k_scan_apply<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred, p.region_start,
+                                                  p.cursor);
+    count_launch(2);
+  }
   if (n) {
     k_part_scatter<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, counts, key_is_hash, shift, p.cursor,
                                                 p.keys, p.counts);
