@@ -45,7 +45,7 @@ struct HostFilter {
   cudaStream_t stream = 0;  // legacy default stream, like the reference
   int log_region = 12;
   bool auto_region = true;
-  uint32_t sparse_max = kDefaultSparseMax;  // regions with <= this many keys go key by key
+  uint32_t sparse_max = GQF_SPARSE_AUTO;  // regions with <= this many keys go key by key
   uint8_t* aux = nullptr;   // status word + miss counter
   Partition part{};
   uint64_t key_cap = 0;
@@ -124,6 +124,28 @@ unsigned long long* merged_ptr(HostFilter* f) { return reinterpret_cast<unsigned
 uint32_t nregions_for(const HostFilter* f, int log_region) {
   uint64_t n = f->h.nslots >> log_region;
   return (uint32_t)(n ? n : 1);
+}
+
+// Key-by-key threshold in use.  The automatic one weighs the key-by-key
+// kernel, whose time follows its busiest region (about k sequential
+// single-key updates of ~25 us each, one thread per region), against a
+// rebuild of every region (~75 ns per region on a GB300): a region of k keys
+// goes key by key while 2 k * 25 us stays under half of nregions * 75 ns.
+uint32_t sparse_max_of(const HostFilter* f) {
+  if (f->sparse_max != GQF_SPARSE_AUTO) return f->sparse_max;
+  const uint32_t t = nregions_for(f, f->log_region) / 1400;
+  return t < 16 ? 16 : t > 256 ? 256 : t;
+}
+
+// The threshold for a batch of n keys.  Under the automatic choice a batch
+// averaging more than half the threshold per region leaves few regions to
+// the key-by-key kernel, whose time is still set by its busiest region, so
+// such batches rebuild every touched region.
+uint32_t sparse_max_for(const HostFilter* f, uint64_t n) {
+  const uint32_t t = sparse_max_of(f);
+  if (f->sparse_max != GQF_SPARSE_AUTO) return t;
+  const uint64_t per_region = n / nregions_for(f, f->log_region);
+  return 2 * per_region <= t ? t : 0;
 }
 
 // Grow partition scratch (stream-ordered, so work already queued keeps its
@@ -218,7 +240,7 @@ int do_bulk_reduce(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flag
   }
   {
     PhaseTimer t(f, GQF_PROF_INSERT, st, n);
-    if (!ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st, f->sparse_max), "rebuild"))
+    if (!ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st, sparse_max_for(f, n)), "rebuild"))
       return -1;
   }
   return 0;
@@ -241,7 +263,7 @@ int do_bulk(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flags, Op o
   }
   {
     PhaseTimer t(f, op == Op::kDelete ? GQF_PROF_DELETE : GQF_PROF_INSERT, st, n);
-    if (!ck(launch_rebuild(f->g, p, op, f->dqf, status_ptr(f), st, f->sparse_max), "rebuild")) return -1;
+    if (!ck(launch_rebuild(f->g, p, op, f->dqf, status_ptr(f), st, sparse_max_for(f, n)), "rebuild")) return -1;
   }
   return 0;
 }
@@ -512,7 +534,7 @@ int gqf_set_sparse_max(QF* qf, uint32_t max_keys) {
 
 int64_t gqf_get_sparse_max(QF* qf) {
   HostFilter* f = lookup(qf);
-  return f ? (int64_t)f->sparse_max : -1;
+  return f ? (int64_t)sparse_max_of(f) : -1;
 }
 
 int gqf_get_region_log(QF* qf) {

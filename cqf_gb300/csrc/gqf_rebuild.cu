@@ -73,6 +73,9 @@ struct Lay {
 };
 
 constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
+// cursor[r] value by which k_sparse hands region r to k_rebuild (the cursors
+// are free once the partition has scattered the keys)
+constexpr uint32_t kHandOff = 0xFFFFFFFFu;
 
 // ----------------------------------------------------- shared-memory image
 
@@ -220,7 +223,9 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom
   const uint32_t r = 2 * blockIdx.x + parity;
   if (r >= p.nregions) return;
   const uint32_t kbeg = p.region_start[r], kend = kbeg + p.region_count[r];
-  if (kend - kbeg <= sparse_max) return;  // empty, or taken by k_sparse
+  if (kbeg == kend) return;
+  // regions up to sparse_max keys belong to k_sparse, unless it handed them on
+  if (kend - kbeg <= sparse_max && p.cursor[r] != kHandOff) return;
   const int tid = threadIdx.x;
 
   const uint64_t base = (uint64_t)r << LOGS;
@@ -592,8 +597,8 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom
 //
 // Before writing anything the thread proves (Serial::sparse_fits) that the
 // region's changes stay inside the window a rebuild would own, [base, base +
-// REG + PUSH); otherwise the region is deferred untouched to the serial
-// fallback.
+// REG + PUSH); otherwise it leaves the region untouched to the rebuild that
+// follows in the same phase.
 template <int LOGS, bool DEL, bool CNT>
 __global__ void __launch_bounds__(128) k_sparse(const quotient_filter* dqf, Partition p, int parity,
                                                 uint32_t sparse_max, uint32_t* status) {
@@ -610,10 +615,7 @@ __global__ void __launch_bounds__(128) k_sparse(const quotient_filter* dqf, Part
   if (!DEL)
     for (uint32_t k = kbeg; k < kbeg + cnt; k++) grow += Serial::insert_growth(CNT ? p.counts[k] : 1);
   if (!S.sparse_fits(region_end, grow, bound)) {
-    const uint32_t at = atomicAdd(&p.deferred[0], 1u);
-    p.deferred[1 + at] = r;
-    atomicOr(status, kStDeferred);
-    if (p.stats) atomicAdd(&p.stats[0], 1ULL);
+    p.cursor[r] = kHandOff;
     return;
   }
   const int shift = 8 + LOGS;

@@ -204,8 +204,11 @@ int gqf_get_region_log(QF* qf);
 
 /* Regions that receive at most max_keys keys of a batch are updated key by
  * key (the reference's single-key algorithms, one thread per region) instead
- * of rebuilt; 0 rebuilds every touched region.  Does not change results, only
- * speed.  Default 32. */
+ * of rebuilt; 0 rebuilds every touched region; GQF_SPARSE_AUTO (the default)
+ * picks nregions / 1400 clamped to [16, 256], for batches averaging at most
+ * half that per region (denser batches rebuild every region).  Does not
+ * change results, only speed.  gqf_get_sparse_max returns the threshold. */
+#define GQF_SPARSE_AUTO 0xFFFFFFFFu
 int gqf_set_sparse_max(QF* qf, uint32_t max_keys);
 int64_t gqf_get_sparse_max(QF* qf);
 

@@ -51,7 +51,7 @@ def test_small_batches_match_canonical_layout(gq, seed, nbits, lr):
     oracle_sound = True
     inserted = []
     with gq.QF(nbits, log_region=lr) as qf:
-        assert qf.sparse_max() == 32
+        assert 16 <= qf.sparse_max() <= 256
         step = 0
         mark = 0.1  # compare at every further tenth of the slots filled
         while used < 0.85 * (1 << nbits):
