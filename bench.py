@@ -314,10 +314,13 @@ def run_gpu(args, wl, rank, world):
         }
     dom = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
     d = kernels[dom]
+    # units of the ncu traffic figures per bulk call: keys probed, regions
+    # staged by the rebuild (both parities; every region holds keys here)
+    nregions = wl.nslots >> qf.region_log()
     units_per_launch = {
         "probe_get": wl.n_get,
-        "rebuild_insert": wl.n_insert / max(1, 2 * len(wl.batches)),
-        "rebuild_delete": wl.n_get / max(1, 2 * ((wl.n_get + wl.batch - 1) // wl.batch)),
+        "rebuild_insert": nregions,
+        "rebuild_delete": nregions,
         "partition": (wl.n_insert + wl.n_get) / max(1, kernels.get("partition", {}).get("calls_per_step", 1)),
     }
     tr = profile_traffic()
