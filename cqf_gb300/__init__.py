@@ -59,6 +59,18 @@ SIGNATURES = {
     "gqf_bulk_insert_noalloc": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_insert_kmers": (_int, [_vp, _vp, _u64, _u32, _u32, _vp]),
     "gqf_kmers_extract": (_int, [_vp, _u64, _u32, _u32, _vp, _vp]),
+    "gqf_set_create": (_int, [_u32, _vp, _u64, ctypes.POINTER(_vp)]),
+    "gqf_set_destroy": (None, [_vp]),
+    "gqf_set_insert": (_int, [_vp, _vp, _vp, _u64, _u8, _vp]),
+    "gqf_set_delete": (_int, [_vp, _vp, _vp, _u64, _u8, _vp]),
+    "gqf_set_get": (_int, [_vp, _vp, _vp, _u64, _vp, _u8, _vp]),
+    "gqf_set_reset": (_int, [_vp, _vp]),
+    "gqf_set_tune": (_int, [_vp, _vp, _vp, _u64, _u8, ctypes.POINTER(ctypes.c_double)]),
+    "gqf_set_config": (_int, [_vp, _int, _u32]),
+    "gqf_set_get_config": (_int, [_vp, ctypes.POINTER(_int), ctypes.POINTER(_u32)]),
+    "gqf_set_export_size": (_u64, [_vp, _u32]),
+    "gqf_set_export": (_int, [_vp, _u32, _vp, _u64]),
+    "gqf_set_get_status": (_int, [_vp, ctypes.POINTER(_u32)]),
     "gqf_server_create": (_int, [_vp, _u64, ctypes.POINTER(_vp)]),
     "gqf_server_submit": (ctypes.c_int64, [_vp, _int, _vp, _u64, _vp, _u32]),
     "gqf_server_poll": (_int, [_vp, ctypes.c_int64]),
@@ -308,6 +320,88 @@ class QF:
     def _ok(self, rc: int):
         if rc != 0:
             raise RuntimeError(last_error())
+
+
+SPARSE_AUTO = 0xFFFFFFFF
+
+
+class FilterSet:
+    """n independent filters served by one launch per phase (gqf_set_* in
+    include/gqf.h).  Batches are device tensors: keys (int64) with CSR
+    offsets (int64, n + 1 entries) on the device."""
+
+    def __init__(self, nbits, max_batch_keys: int):
+        self.L = load()
+        nb = np.ascontiguousarray(nbits, dtype=np.int32)
+        self.n = int(nb.size)
+        self.nbits = nb.copy()
+        h = _vp()
+        if self.L.gqf_set_create(self.n, nb.ctypes.data, int(max_batch_keys), ctypes.byref(h)) != 0:
+            raise RuntimeError("gqf_set_create failed: " + last_error())
+        self.h = h
+
+    def _ok(self, rc):
+        if rc != 0:
+            raise RuntimeError(last_error())
+
+    def insert(self, keys, offsets, n=None, flags=QF_NO_LOCK, stream=None):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_set_insert(self.h, _ptr(keys), _ptr(offsets), n, flags, _stream_ptr(stream)))
+
+    def delete(self, keys, offsets, n=None, flags=QF_NO_LOCK, stream=None):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_set_delete(self.h, _ptr(keys), _ptr(offsets), n, flags, _stream_ptr(stream)))
+
+    def get(self, keys, offsets, counts, n=None, flags=0, stream=None):
+        n = keys.numel() if n is None else n
+        self._ok(self.L.gqf_set_get(self.h, _ptr(keys), _ptr(offsets), n, _ptr(counts), flags, _stream_ptr(stream)))
+
+    def reset(self, stream=None):
+        self._ok(self.L.gqf_set_reset(self.h, _stream_ptr(stream)))
+
+    def tune(self, keys, offsets, n=None, flags=QF_NO_LOCK) -> float:
+        """Picks region size and key-by-key threshold by timing inserts of
+        this batch; leaves the set empty.  Returns the best insert time (ms)."""
+        n = keys.numel() if n is None else n
+        ms = ctypes.c_double(0)
+        self._ok(self.L.gqf_set_tune(self.h, _ptr(keys), _ptr(offsets), n, flags, ctypes.byref(ms)))
+        return ms.value
+
+    def config(self, log_region: int | None = None, sparse_max: int | None = None):
+        lr, sp = _int(0), _u32(0)
+        self._ok(self.L.gqf_set_get_config(self.h, ctypes.byref(lr), ctypes.byref(sp)))
+        if log_region is None and sparse_max is None:
+            return {"log_region": lr.value, "sparse_max": sp.value}
+        self._ok(self.L.gqf_set_config(self.h, lr.value if log_region is None else log_region,
+                                       sp.value if sparse_max is None else sparse_max))
+
+    def export(self, i: int) -> np.ndarray:
+        size = int(self.L.gqf_set_export_size(self.h, i))
+        out = np.zeros(size, dtype=np.uint8)
+        self._ok(self.L.gqf_set_export(self.h, i, out.ctypes.data, size))
+        return out
+
+    def status(self) -> int:
+        s = _u32(0)
+        self._ok(self.L.gqf_set_get_status(self.h, ctypes.byref(s)))
+        return int(s.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gqf_set_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 OP_GET, OP_INSERT, OP_DELETE, OP_INSERT_REDUCE = 0, 1, 2, 3

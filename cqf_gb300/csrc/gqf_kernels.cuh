@@ -39,6 +39,52 @@ struct Partition {
 
 enum class Op : int { kInsert = 0, kDelete = 1 };
 
+// Where the regions of one rebuild launch live.  Region R of the launch is
+// region r of the filter `q` with geometry `g`.
+struct OneFilter {  // R = r
+  Geom g;
+  const quotient_filter* dqf;
+  __device__ __forceinline__ bool locate(uint32_t R, int, Geom* gg, uint32_t* r,
+                                         const quotient_filter** q) const {
+    *gg = g;
+    *r = R;
+    *q = dqf;
+    return true;
+  }
+};
+
+// Many filters in one launch: their regions are numbered one after the
+// other, filter f's from region_base[f]; each filter's count is rounded up to
+// an even number so that parities agree (the padding regions are empty).
+struct FilterSet {
+  const quotient_filter* qfs;    // n descriptors in device memory
+  const uint32_t* region_base;   // n + 1 entries, device memory
+  uint32_t n;
+  __device__ __forceinline__ bool locate(uint32_t R, int log_region, Geom* gg, uint32_t* r,
+                                         const quotient_filter** q) const {
+    uint32_t lo = 0, hi = n;  // the last f with region_base[f] <= R
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (region_base[mid] <= R) lo = mid;
+      else hi = mid;
+    }
+    const quotient_filter* f = qfs + lo;
+    const uint32_t rr = R - region_base[lo];
+    const uint64_t nreg = f->nslots >> log_region;
+    if (rr >= (nreg ? nreg : 1)) return false;
+    gg->blocks = f->blocks;
+    gg->nslots = f->nslots;
+    gg->xnslots = f->xnslots;
+    gg->nblocks = f->nblocks;
+    gg->range = f->range;
+    gg->mask = f->range - 1;
+    gg->nbits = f->nbits;
+    *r = rr;
+    *q = f;
+    return true;
+  }
+};
+
 // What other translation units of the library may see of a filter.
 struct FilterView {
   Geom g;
@@ -65,6 +111,10 @@ cudaError_t launch_bulk_get_misses(const Geom& g, const uint64_t* keys, uint64_t
 // hash -> per-region counts -> prefix -> scatter of region-local hashes.
 cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
                              int key_is_hash, uint32_t* status, cudaStream_t st);
+
+// Exclusive scan of p.region_count into p.region_start and p.cursor (and
+// region_start[nregions] = total), using p.deferred as scratch.
+cudaError_t launch_region_scan(const Partition& p, cudaStream_t st);
 
 // The same for (hash, count) pairs whose number n_dev the device holds (n
 // bounds it): hashes are taken as they are, counts land in p.counts.

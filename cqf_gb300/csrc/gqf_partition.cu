@@ -169,6 +169,15 @@ int grid_for(uint64_t n) {
 
 }  // namespace
 
+cudaError_t launch_region_scan(const Partition& p, cudaStream_t st) {
+  // the chunk sums use the deferred list as scratch: the rebuild resets it
+  const uint32_t chunks = (p.nregions + kScanChunk - 1) / kScanChunk;
+  k_scan_sums<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred);
+  k_scan_apply<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred, p.region_start, p.cursor);
+  count_launch(2);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_partition(const Geom& g, const Partition& p, const uint64_t* keys, uint64_t n,
                              int key_is_hash, uint32_t* status, cudaStream_t st) {
   return launch_partition_counted(g, p, keys, nullptr, n, nullptr, key_is_hash, status, st);
@@ -184,14 +193,8 @@ cudaError_t launch_partition_counted(const Geom& g, const Partition& p, const ui
     k_part_count<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, key_is_hash, shift, p.region_count, status);
     count_launch();
   }
-  {
-    // the chunk sums use the deferred list as scratch: the rebuild resets it
-    const uint32_t chunks = (p.nregions + kScanChunk - 1) / kScanChunk;
-    k_scan_sums<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred);
-    k_scan_apply<<<chunks, kScanThreads, 0, st>>>(p.region_count, p.nregions, p.deferred, p.region_start,
-                                                  p.cursor);
-    count_launch(2);
-  }
+  e = launch_region_scan(p, st);
+  if (e != cudaSuccess) return e;
   if (n) {
     k_part_scatter<<<grid_for(n), 256, 0, st>>>(g, keys, n, n_dev, counts, key_is_hash, shift, p.cursor,
                                                 p.keys, p.counts);

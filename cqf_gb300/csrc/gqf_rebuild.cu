@@ -1,712 +1,8 @@
-// Region rebuild: the bulk insert / delete hot path.
-//
-// The reference applies a batch with one thread per 8192-slot region that
-// inserts its sorted keys one at a time, shifting slots byte by byte
-// (insert_from_buffers_hashed / delete_from_buffers_hashed,
-// src/gqf.cu:2759-2906, two launches: even regions then odd).  The layout
-// that produces is canonical: it depends only on the multiset of
-// (quotient, remainder, count), never on the order of operations.  So this
-// kernel rebuilds a region's layout in one pass instead:
-//
-//   * one CTA per region of 2^LOGS quotients, even regions then odd ones (the
-//     reference's schedule), so two CTAs never touch the same slots;
-//   * the CTA stages a window of LOGS-region + PUSH slots in shared memory
-//     (the region plus the head of the next one, which its growth may push);
-//   * it groups the region's new keys by quotient with a counting sort in
-//     shared memory, merges them with the old counters of the touched runs
-//     only (decode_counter / encode_counter, src/gqf.cu:1216-1345), and
-//     recomputes every run position with one block-wide max-plus scan:
-//     end(q) = max(q + L_q - 1, end(prev) + L_q);
-//   * untouched runs move byte-parallel (every slot knows its run's shift);
-//   * it writes back only the blocks that changed.
-//
-// A rebuild whose changes would reach past the window (a cluster longer than
-// PUSH slots, or the end of the table) is deferred: nothing is written and the
-// region is applied afterwards by a single-thread serial pass built from the
-// reference's own single-key algorithms (gqf_device.cuh), which handles any
-// cluster length and reports a full table like the reference does.
-#include "gqf_kernels.cuh"
+// Region rebuild for one filter (the instantiation for a set of filters is
+// in gqf_set.cu); the kernels are in gqf_rebuild_impl.cuh.
+#include "gqf_rebuild_impl.cuh"
 
 namespace gqf {
-namespace {
-
-constexpr int kNeg = -(1 << 28);  // "minus infinity" of the max-plus scan
-
-template <int LOGS>
-struct Cfg;
-template <>
-struct Cfg<11> { static constexpr int PUSH = 1024, KMAX = 2048, MINB = 4; };
-template <>
-struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 3; };
-template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 1; };
-
-template <int LOGS, bool CNT>
-struct Lay {
-  static constexpr int NT = 256;
-  static constexpr int REG = 1 << LOGS;
-  static constexpr int PUSH = Cfg<LOGS>::PUSH;
-  static constexpr int KMAX = Cfg<LOGS>::KMAX;
-  static constexpr int WIN = REG + PUSH;
-  static constexpr int WB = WIN / 64;
-  static constexpr int QPT = WIN / NT;
-  static constexpr int KCW = REG / 2 + 2;  // packed 16-bit per-quotient key counters
-  static_assert(WIN % NT == 0 && (REG / 2) % NT == 0, "work splits evenly over threads");
-  static_assert(PUSH < REG, "a window must not reach the region after next");
-  static_assert(WIN + PUSH + 64 < 32767, "window positions fit int16");
-  // shared memory carve-up (bytes)
-  static constexpr int IMG = WB * 96;
-  static constexpr int OFF_IMG0 = 0;
-  static constexpr int OFF_IMG1 = OFF_IMG0 + IMG;
-  static constexpr int OFF_KG = OFF_IMG1 + IMG;                  // u32[KMAX] keys grouped by quotient
-  static constexpr int OFF_KC = OFF_KG + KMAX * 4;               // u32[KCW]
-  static constexpr int OFF_RPOS = OFF_KC + KCW * 4;              // u16[WIN + 8] old run ends by rank
-  static constexpr int OFF_PREF = OFF_RPOS + (WIN + 8) * 2;      // u16[WIN] lengths, then ends + 1
-  static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8] old start, then shift
-  static constexpr int OFF_USED = OFF_DELTA + (WIN + 8) * 2;     // u32[WIN / 32] old run slots
-  static constexpr int OFF_NOCC = (OFF_USED + WIN / 8 + 7) & ~7; // u64[WB] new occupieds
-  static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
-  static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
-  static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;     // u16[WB + 8]
-  static constexpr int OFF_KN = (OFF_RRANK + (WB + 8) * 2 + 3) & ~3;  // u32[KMAX] key counts (CNT)
-  static constexpr int BYTES = OFF_KN + (CNT ? KMAX * 4 : 0);
-};
-
-constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
-// cursor[r] value by which k_sparse hands region r to k_rebuild (the cursors
-// are free once the partition has scattered the keys)
-constexpr uint32_t kHandOff = 0xFFFFFFFFu;
-
-// ----------------------------------------------------- shared-memory image
-
-struct Img {
-  uint8_t* p;
-  __device__ uint8_t& slot(int i) const { return p[(i >> 6) * 96 + 32 + (i & 63)]; }
-  __device__ unsigned long long& occ(int w) const { return *reinterpret_cast<unsigned long long*>(p + w * 96); }
-  __device__ unsigned long long& run(int w) const { return *reinterpret_cast<unsigned long long*>(p + w * 96 + 8); }
-  __device__ uint32_t& off(int w) const { return *reinterpret_cast<uint32_t*>(p + w * 96 + 16); }
-  __device__ int is_end(int i) const { return (int)((run(i >> 6) >> (i & 63)) & 1ULL); }
-};
-
-// Merge one run's old counters with the run's new keys (sorted by remainder;
-// each key counts once, or cnts[j] times when cnts is given) and return the
-// new run length; with WRITE, also emit the bytes at out[pos..].
-template <bool DEL, bool WRITE>
-__device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* keys, const uint32_t* cnts,
-                         int ki, int kj, Img out, int pos) {
-  auto get = [&](uint64_t i) -> uint64_t { return cur.slot((int)i); };
-  auto end = [&](uint64_t i) -> int { return cur.is_end((int)i); };
-  const uint64_t lim = (uint64_t)e + 1;  // the walk never leaves the run [s, e]
-  int total = 0;
-  bool have_old = has_old;
-  int opos = s;
-  uint32_t orem = 0;
-  uint64_t ocnt = 0;
-  int oend = 0;
-  if (have_old) oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
-  int j = ki;
-  uint8_t enc[16];
-  while (have_old || j < kj) {
-    uint32_t nrem = 0;
-    uint64_t ncnt = 0;
-    int jn = j;
-    if (j < kj) {
-      nrem = keys[j] & 255u;
-      while (jn < kj && (keys[jn] & 255u) == nrem) {
-        ncnt += cnts ? cnts[jn] : 1u;
-        jn++;
-      }
-    }
-    bool take_old = have_old && (j >= kj || orem < nrem);
-    bool both = have_old && j < kj && orem == nrem;
-    if (take_old) {
-      int len = oend - opos + 1;
-      if (WRITE)
-        for (int t = 0; t < len; t++) out.slot(pos + total + t) = cur.slot(opos + t);
-      total += len;
-    } else {
-      uint64_t c = both ? (DEL ? (ocnt > ncnt ? ocnt - ncnt : 0) : ocnt + ncnt) : (DEL ? 0 : ncnt);
-      int len = encode_counter(nrem, c, enc);
-      if (WRITE)
-        for (int t = 0; t < len; t++) out.slot(pos + total + t) = enc[t];
-      total += len;
-      j = jn;
-    }
-    if (take_old || both) {
-      if (cur.is_end(oend) || oend >= e) {
-        have_old = false;
-      } else {
-        opos = oend + 1;
-        oend = (int)decode_counter(get, end, (uint64_t)opos, &orem, &ocnt, lim);
-      }
-    }
-  }
-  return total;
-}
-
-// Block-wide exclusive scan of max-plus maps f(x) = max(a, x + b).
-template <int NT>
-__device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int ia = a, ib = b;  // inclusive
-  for (int o = 1; o < 32; o <<= 1) {
-    int pa = __shfl_up_sync(0xffffffffu, ia, o);
-    int pb = __shfl_up_sync(0xffffffffu, ib, o);
-    if (lane >= o) {  // (pa,pb) first, then (ia,ib)
-      ia = max(ia, pa + ib);
-      ib = pb + ib;
-    }
-  }
-  if (lane == 31) { sa[wid] = ia; sb[wid] = ib; }
-  __syncthreads();
-  if (wid == 0) {
-    int wa = lane < NT / 32 ? sa[lane] : kNeg, wb = lane < NT / 32 ? sb[lane] : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      int pa = __shfl_up_sync(0xffffffffu, wa, o);
-      int pb = __shfl_up_sync(0xffffffffu, wb, o);
-      if (lane >= o) { wa = max(wa, pa + wb); wb = pb + wb; }
-    }
-    sa[lane] = wa;
-    sb[lane] = wb;
-  }
-  __syncthreads();
-  int ea = __shfl_up_sync(0xffffffffu, ia, 1), eb = __shfl_up_sync(0xffffffffu, ib, 1);
-  if (lane == 0) { ea = kNeg; eb = 0; }
-  if (wid > 0) {
-    int pa = sa[wid - 1], pb = sb[wid - 1];
-    ea = max(ea, pa + eb);
-    eb = pb + eb;
-  }
-  a = ea;
-  b = eb;
-  __syncthreads();
-}
-
-// Block-wide exclusive sum; returns this thread's prefix and the total.
-template <int NT>
-__device__ int scan_sum(int v, int* tmp, int* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    int t = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += t;
-  }
-  if (lane == 31) tmp[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int w = lane < NT / 32 ? tmp[lane] : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += t;
-    }
-    tmp[lane] = w;
-  }
-  __syncthreads();
-  int r = x - v + (wid ? tmp[wid - 1] : 0);
-  *total = tmp[NT / 32 - 1];
-  __syncthreads();
-  return r;
-}
-
-// CNT: the batch carries a multiplicity per key (p.counts), as produced by
-// the duplicate-merging pass of bulk_insert_reduce.
-template <int LOGS, bool DEL, bool CNT>
-__global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Geom g, Partition p, int parity,
-                                                                             uint32_t sparse_max,
-                                                                             uint32_t* status) {
-  using L = Lay<LOGS, CNT>;
-  constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
-  extern __shared__ __align__(128) uint8_t sm[];
-  __shared__ int s_i[8];
-  __shared__ int sa[32], sb[32];
-
-  const uint32_t r = 2 * blockIdx.x + parity;
-  if (r >= p.nregions) return;
-  const uint32_t kbeg = p.region_start[r], kend = kbeg + p.region_count[r];
-  if (kbeg == kend) return;
-  // regions up to sparse_max keys belong to k_sparse, unless it handed them on
-  if (kend - kbeg <= sparse_max && p.cursor[r] != kHandOff) return;
-  const int tid = threadIdx.x;
-
-  const uint64_t base = (uint64_t)r << LOGS;
-  const uint64_t bw0 = base >> 6;
-  const int wb = (int)min((uint64_t)WB, g.nblocks - bw0);
-  const int wslots = wb * 64;
-  const int win_valid = (int)min((uint64_t)wslots, g.xnslots - base);
-  const int win_q = (int)min((uint64_t)WIN, g.nslots - base);
-  const int wq_words = (win_q + 63) >> 6;
-  const int nq = (int)min((uint64_t)REG, g.nslots - base);
-
-  uint32_t* kg = reinterpret_cast<uint32_t*>(sm + L::OFF_KG);
-  uint32_t* kc = reinterpret_cast<uint32_t*>(sm + L::OFF_KC);
-  uint16_t* rpos = reinterpret_cast<uint16_t*>(sm + L::OFF_RPOS);
-  uint16_t* pref = reinterpret_cast<uint16_t*>(sm + L::OFF_PREF);
-  int16_t* delta = reinterpret_cast<int16_t*>(sm + L::OFF_DELTA);
-  uint32_t* used = reinterpret_cast<uint32_t*>(sm + L::OFF_USED);
-  unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
-  unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
-  uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
-  uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
-  uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
-
-  // ---- stage the window (wb blocks of 96 bytes) into image 0
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(g.blocks + bw0);
-    uint4* dst = reinterpret_cast<uint4*>(sm + L::OFF_IMG0);
-    for (int i = tid; i < wb * 6; i += NT) dst[i] = src[i];
-  }
-  __syncthreads();
-  const int c0 = (int)Img{sm + L::OFF_IMG0}.off(0) - 1;  // last slot used by earlier regions' runs
-  // The previous region's runs fill the whole window: every run of this
-  // region lies beyond it, so only the serial path can place them.  (This
-  // also keeps all window positions far below the 16-bit tables' range.)
-  bool deferred = c0 + 1 >= win_valid;
-  const bool multi = kend - kbeg > (uint32_t)KMAX;
-  int cur = 0;
-  bool changed = false;
-
-  auto kcnt = [&](int q) -> int { return (int)((kc[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu); };
-  // runends of word w that lie after c0
-  auto runs_after_c0 = [&](Img C, int w) -> unsigned long long {
-    unsigned long long rw = C.run(w);
-    int lo = 64 * w;
-    if (c0 >= lo + 63) return 0ULL;
-    if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
-    return rw;
-  };
-
-  for (uint32_t kr = kbeg; kr < kend && !deferred; kr += KMAX) {
-    const int nk = (int)min((uint32_t)KMAX, kend - kr);
-    const Img C{sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0)};
-    const Img N{sm + (cur ? L::OFF_IMG0 : L::OFF_IMG1)};
-
-    // ---- group this round's keys by quotient (counting sort in shared memory)
-    for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
-    for (int i = tid; i < WB; i += NT) { nocc[i] = 0; tch[i] = 0; }
-    for (int i = tid; i < WIN / 32; i += NT) used[i] = 0;
-    __syncthreads();
-    for (int i = tid; i < nk; i += NT) {
-      uint32_t q = p.keys[kr + i] >> 8;
-      atomicAdd(&kc[q >> 1], 1u << ((q & 1) * 16));
-    }
-    __syncthreads();
-    {  // exclusive prefix over the REG counters, 2 per word
-      constexpr int WPT = (REG / 2) / NT;
-      int a = tid * WPT, sum = 0;
-      for (int w = a; w < a + WPT; w++) sum += (int)(kc[w] & 0xFFFFu) + (int)(kc[w] >> 16);
-      int tot;
-      int run = scan_sum<NT>(sum, sa, &tot);
-      for (int w = a; w < a + WPT; w++) {
-        uint32_t v = kc[w];
-        uint32_t lo = (uint32_t)run;
-        run += (int)(v & 0xFFFFu);
-        uint32_t hi = (uint32_t)run;
-        run += (int)(v >> 16);
-        kc[w] = lo | (hi << 16);
-      }
-    }
-    __syncthreads();
-    for (int i = tid; i < nk; i += NT) {
-      uint32_t key = p.keys[kr + i];
-      uint32_t q = key >> 8;
-      uint32_t sh = (q & 1) * 16;
-      uint32_t old = atomicAdd(&kc[q >> 1], 1u << sh);
-      kg[(old >> sh) & 0xFFFFu] = key;
-      if (CNT) kn[(old >> sh) & 0xFFFFu] = p.counts[kr + i];
-    }
-    // now the keys of quotient q are kg[q ? kcnt(q-1) : 0, kcnt(q))
-
-    // ---- rank tables of the current image: per window word, the occupied
-    // quotients and the runends after c0 before it (one packed block scan)
-    {
-      int packed = 0;
-      if (tid < WB) {
-        const int co = tid < wq_words ? __popcll(C.occ(tid)) : 0;
-        const int cr = tid < wb ? __popcll(runs_after_c0(C, tid)) : 0;
-        packed = co | (cr << 16);
-      }
-      int tot;
-      const int ex = scan_sum<NT>(packed, sa, &tot);
-      if (tid < WB) {
-        orank[tid] = (uint16_t)(ex & 0xFFFF);
-        rrank[tid] = (uint16_t)(ex >> 16);
-      }
-      if (tid == 0) { s_i[0] = tot >> 16; s_i[1] = tot & 0xFFFF; }  // visible runends, occupied quotients
-    }
-    __syncthreads();
-    const int nvis = s_i[0], nold = s_i[1];
-    // Each thread owns QPT consecutive slots / quotients from here on, so
-    // ranks, run ends and shifts carry from one to the next in registers.
-    const int ca = tid * QPT;
-    {  // rpos[k] = the k-th runend after c0, for this thread's slots
-      const int cb = min(ca + QPT, wslots);
-      int x = ca;
-      while (x < cb) {
-        const int w = x >> 6;
-        const int xe = min(cb, 64 * w + 64);
-        unsigned long long m = runs_after_c0(C, w);
-        int k = rrank[w] + __popcll(m & ((1ULL << (x & 63)) - 1ULL));
-        m &= ~0ULL << (x & 63);
-        if (xe < 64 * w + 64) m &= (1ULL << (xe & 63)) - 1ULL;
-        while (m) {
-          rpos[k++] = (uint16_t)(64 * w + __ffsll((long long)m) - 1);
-          m &= m - 1;
-        }
-        x = xe;
-      }
-    }
-    __syncthreads();
-
-    const int fake0 = win_valid + 16;
-    auto runpos = [&](int k) -> int { return k < nvis ? (int)rpos[k] : fake0 + (k - nvis); };
-    auto rank_of = [&](int q) -> int {
-      return (int)orank[q >> 6] + __popcll(C.occ(q >> 6) & ((1ULL << (q & 63)) - 1ULL));
-    };
-
-    // ---- merge tasks: new length of every touched quotient (first key of
-    // each group), before the positions are scanned
-    bool my_defer = false;
-    for (int i = tid; i < nk; i += NT) {
-      const uint32_t q = kg[i] >> 8;
-      if (i > 0 && (kg[i - 1] >> 8) == q) continue;
-      const int ks = i, ke = kcnt((int)q);
-      atomicOr(&tch[q >> 6], 1ULL << (q & 63));
-      const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
-      int s = 0, e = -1;
-      if (occ) {
-        const int k = rank_of((int)q);
-        e = runpos(k);
-        s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
-      }
-      if (occ && e >= win_valid) {
-        my_defer = true;
-        continue;
-      }
-      for (int a = ks + 1; a < ke; a++) {  // the quotient's keys by remainder
-        const uint32_t v = kg[a];
-        const uint32_t vc = CNT ? kn[a] : 0u;
-        int b = a;
-        while (b > ks && kg[b - 1] > v) {
-          kg[b] = kg[b - 1];
-          if (CNT) kn[b] = kn[b - 1];
-          b--;
-        }
-        kg[b] = v;
-        if (CNT) kn[b] = vc;
-      }
-      pref[q] = (uint16_t)merge_run<DEL, false>(C, occ, s, e, kg, kn, ks, ke, N, 0);
-    }
-    if (__syncthreads_or(my_defer)) { deferred = true; break; }
-
-    // ---- this thread's quotients: old runs, new lengths, composed max-plus map
-    const int qb_ = min(ca + QPT, win_q);
-    const int k0 = ca < win_q ? rank_of(ca) : nold;
-    int fa = kNeg, fb = 0;
-    {
-      int k = k0;
-      int pe = k ? runpos(k - 1) : c0;
-      int ne = runpos(k);  // end of the next old run
-      unsigned long long ow = 0, tw = 0;
-      int cw = -1;
-      uint32_t ubits = 0;  // used-slot bits of 32-bit word uw
-      int uw = -1;
-      for (int q = ca; q < qb_; q++) {
-        if ((q >> 6) != cw) {
-          cw = q >> 6;
-          ow = C.occ(cw);
-          tw = q < nq ? tch[cw] : 0ULL;
-        }
-        int len = 0;
-        if ((ow >> (q & 63)) & 1ULL) {
-          const int e = ne;
-          ne = runpos(k + 1);
-          const int s = max(q, pe + 1);
-          len = e - s + 1;
-          delta[k] = (int16_t)s;
-          const int last = min(e, wslots - 1);
-          for (int x = s; x <= last; x++) {  // mark the run's slots
-            if ((x >> 5) != uw) {
-              if (ubits) atomicOr(&used[uw], ubits);
-              uw = x >> 5;
-              ubits = 0;
-            }
-            ubits |= 1u << (x & 31);
-          }
-          pe = e;
-          k++;
-        }
-        if ((tw >> (q & 63)) & 1ULL) len = pref[q];
-        pref[q] = (uint16_t)len;
-        if (len > 0) { fa = max(q + len - 1, fa + len); fb += len; }
-      }
-      if (ubits) atomicOr(&used[uw], ubits);
-    }
-
-    // ---- run positions: one block-wide max-plus scan over the quotients
-    scan_maps<NT>(fa, fb, sa, sb);
-    // ---- clear the next image; keep the previous region's spill
-    {
-      uint4* dst = reinterpret_cast<uint4*>(N.p);
-      for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
-    }
-    __syncthreads();
-    for (int sl = tid; sl <= c0 && sl < wslots; sl += NT) N.slot(sl) = C.slot(sl);
-    for (int w = tid; w < wb && 64 * w <= c0; w += NT) {
-      int nb = c0 - 64 * w;  // bits 0..nb belong to the previous region's runs
-      N.run(w) = nb >= 63 ? C.run(w) : (C.run(w) & ((2ULL << nb) - 1ULL));
-    }
-    __syncthreads();
-    // ---- apply: new ends, runend bits, occupancy, shift of every old run
-    {
-      int x = max(fa, c0 + fb);  // end of all runs before this thread's first quotient
-      int k = k0;
-      unsigned long long occ_bits = 0, ow = 0, tw = 0;
-      int occ_word = ca >> 6, cw = -1;
-      unsigned long long ebits = 0;  // new runend bits of window word ew
-      int ew = -1;
-      for (int q = ca; q < qb_; q++) {
-        if ((q >> 6) != cw) {
-          if (cw >= 0 && occ_bits) atomicOr(&nocc[occ_word], occ_bits);
-          occ_bits = 0;
-          cw = occ_word = q >> 6;
-          ow = C.occ(cw);
-          tw = q < nq ? tch[cw] : 0ULL;
-        }
-        const int len = pref[q];
-        const int ns = max(q, x + 1);
-        if (len > 0) {
-          x = ns + len - 1;
-          occ_bits |= 1ULL << (q & 63);
-          if (x < wslots) {
-            if ((x >> 6) != ew) {
-              if (ebits) atomicOr(&N.run(ew), ebits);
-              ew = x >> 6;
-              ebits = 0;
-            }
-            ebits |= 1ULL << (x & 63);
-          }
-        }
-        if ((ow >> (q & 63)) & 1ULL) {
-          delta[k] = ((tw >> (q & 63)) & 1ULL) ? kTouched : (int16_t)(ns - delta[k]);
-          k++;
-        }
-        pref[q] = (uint16_t)(x + 1);
-      }
-      if (occ_bits) atomicOr(&nocc[occ_word], occ_bits);
-      if (ebits) atomicOr(&N.run(ew), ebits);
-    }
-    __syncthreads();
-    {
-      const int e_old = nold ? runpos(nold - 1) : c0;
-      const int e_new = (int)pref[win_q - 1] - 1;
-      // A change that reaches the window's end would move runs this CTA does
-      // not hold (or overflow the table): leave the region to the serial pass.
-      if (e_new != e_old && max(e_new, e_old) >= win_valid) { deferred = true; break; }
-    }
-    // ---- merge tasks again, now writing the touched runs at their new start
-    for (int i = tid; i < nk; i += NT) {
-      const uint32_t q = kg[i] >> 8;
-      if (i > 0 && (kg[i - 1] >> 8) == q) continue;
-      if (!((nocc[q >> 6] >> (q & 63)) & 1ULL)) continue;  // deleted entirely
-      const int ks = i, ke = kcnt((int)q);
-      const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
-      int s = 0, e = -1;
-      if (occ) {
-        const int k = rank_of((int)q);
-        e = runpos(k);
-        s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
-      }
-      const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
-      merge_run<DEL, true>(C, occ, s, e, kg, kn, ks, ke, N, ns);
-    }
-    // ---- slot pass: this thread's slots move by their run's shift
-    {
-      const int cb = min(ca + QPT, wslots);
-      if (ca < cb) {
-        int w = ca >> 6;
-        unsigned long long m = runs_after_c0(C, w);
-        int k = rrank[w] + __popcll(m & ((1ULL << (ca & 63)) - 1ULL));
-        for (int sl = ca; sl < cb; sl++) {
-          if ((sl >> 6) != w) {
-            w = sl >> 6;
-            m = runs_after_c0(C, w);
-          }
-          if ((used[sl >> 5] >> (sl & 31)) & 1u) {
-            const int d = delta[k];
-            if (d != kTouched) {
-              const int t = sl + d;
-              if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
-            }
-          }
-          k += (int)((m >> (sl & 63)) & 1ULL);
-        }
-      }
-    }
-    __syncthreads();
-    // ---- block headers: occupieds and offsets
-    for (int w = tid; w < wb; w += NT) {
-      N.occ(w) = w < wq_words ? nocc[w] : 0ULL;
-      if (w == 0) {
-        N.off(0) = C.off(0);
-      } else {
-        const int x = min(64 * w - 1, win_q - 1);
-        const int E = (int)pref[x] - 1;
-        N.off(w) = E >= win_valid ? C.off(w) : (uint32_t)max(0, E - 64 * w + 1);
-      }
-    }
-    __syncthreads();
-    cur ^= 1;
-    changed = true;
-  }
-
-  if (deferred) {
-    if (tid == 0) {
-      uint32_t at = atomicAdd(&p.deferred[0], 1u);
-      p.deferred[1 + at] = r;
-      atomicOr(status, kStDeferred);
-      if (p.stats) atomicAdd(&p.stats[0], 1ULL);
-    }
-    return;
-  }
-  if (!changed) return;
-  // ---- write back the blocks that differ from what was loaded
-  {
-    const uint4* fin = reinterpret_cast<const uint4*>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
-    const uint4* org = reinterpret_cast<const uint4*>(sm + L::OFF_IMG0);
-    uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0);
-    for (int w = tid; w < wb; w += NT) {
-      bool diff = multi;  // after several rounds the loaded image is gone
-      if (!diff)
-        for (int c = 0; c < 6; c++) {
-          uint4 a = fin[w * 6 + c], b = org[w * 6 + c];
-          diff |= (a.x != b.x) | (a.y != b.y) | (a.z != b.z) | (a.w != b.w);
-        }
-      if (diff)
-        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
-    }
-  }
-}
-
-// Sparse regions.  The rebuild visits every quotient and slot of its window
-// whatever the number of keys, so a region holding only a few keys (a small
-// batch, or a large table) is cheaper to update key by key: one thread per
-// region applies the reference's single-key algorithms (gqf_device.cuh,
-// src/gqf.cu:1523 insert1, :1768 insert, :1876 _remove) in place, as the
-// reference's insert_from_buffers_hashed does for every region
-// (src/gqf.cu:2759-2804).
-//
-// Before writing anything the thread proves (Serial::sparse_fits) that the
-// region's changes stay inside the window a rebuild would own, [base, base +
-// REG + PUSH); otherwise it leaves the region untouched to the rebuild that
-// follows in the same phase.
-template <int LOGS, bool DEL, bool CNT>
-__global__ void __launch_bounds__(128) k_sparse(const quotient_filter* dqf, Partition p, int parity,
-                                                uint32_t sparse_max, uint32_t* status) {
-  const uint32_t r = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + parity;
-  if (r >= p.nregions) return;
-  const uint32_t cnt = p.region_count[r];
-  if (cnt == 0 || cnt > sparse_max) return;
-  const Serial S(dqf);
-  const uint32_t kbeg = p.region_start[r];
-  const uint64_t base = (uint64_t)r << LOGS;
-  const uint64_t region_end = base + (1ULL << LOGS);  // a block boundary below nslots
-  const uint64_t bound = min(base + (uint64_t)Lay<LOGS, false>::WIN, min(S.xnslots, 64 * S.nblocks));
-  uint64_t grow = 0;  // slots the batch may add (0 for deletes)
-  if (!DEL)
-    for (uint32_t k = kbeg; k < kbeg + cnt; k++) grow += Serial::insert_growth(CNT ? p.counts[k] : 1);
-  if (!S.sparse_fits(region_end, grow, bound)) {
-    p.cursor[r] = kHandOff;
-    return;
-  }
-  const int shift = 8 + LOGS;
-  for (uint32_t k = kbeg; k < kbeg + cnt; k++) {
-    const uint64_t h = ((uint64_t)r << shift) | p.keys[k];
-    if (DEL) {
-      S.remove(h, 1);
-    } else {
-      const uint64_t c = CNT ? p.counts[k] : 1;
-      const int rc = c == 1 ? S.insert1(h) : S.insert(h, c);
-      if (rc < 0) atomicOr(status, kStFull);
-    }
-  }
-}
-
-// Serial fallback for deferred regions: the reference's single-key
-// operations, one key at a time, in region order.
-__global__ void k_fallback(quotient_filter* dqf, Partition p, int del, uint32_t* status) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  uint32_t n = p.deferred[0];
-  if (n == 0) return;
-  // ascending region order (insertion sort; the list is short)
-  uint32_t* ids = p.deferred + 1;
-  for (uint32_t i = 1; i < n; i++) {
-    uint32_t v = ids[i];
-    uint32_t j = i;
-    while (j > 0 && ids[j - 1] > v) { ids[j] = ids[j - 1]; j--; }
-    ids[j] = v;
-  }
-  Serial S(dqf);
-  const int shift = 8 + p.log_region;
-  for (uint32_t i = 0; i < n; i++) {
-    uint32_t r = ids[i];
-    if (p.stats) p.stats[1] += p.region_count[r];
-    for (uint32_t k = p.region_start[r]; k < p.region_start[r] + p.region_count[r]; k++) {
-      uint64_t h = ((uint64_t)r << shift) | p.keys[k];
-      uint64_t c = p.counts ? p.counts[k] : 1;
-      if (del) {
-        for (uint64_t t = 0; t < c; t++) S.remove(h, 1);
-      } else {
-        int rc = c == 1 ? S.insert1(h) : S.insert(h, c);
-        if (rc < 0) atomicOr(status, kStFull);
-      }
-    }
-  }
-}
-
-template <int LOGS, bool DEL, bool CNT>
-void configure() {
-  static bool done = false;  // per instantiation
-  if (done) return;
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       Lay<LOGS, CNT>::BYTES);
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  done = true;
-}
-
-template <int LOGS>
-cudaError_t run_phases(const Geom& g, const Partition& p, Op op, const quotient_filter* dqf, uint32_t sparse_max,
-                       uint32_t* status, cudaStream_t st) {
-  const bool cnt = p.counts != nullptr;
-  if (op == Op::kDelete && cnt) return cudaErrorInvalidValue;  // deletes carry no counts
-  if (op == Op::kDelete) configure<LOGS, true, false>();
-  else if (cnt) configure<LOGS, false, true>();
-  else configure<LOGS, false, false>();
-  const uint32_t half = (p.nregions + 1) / 2;
-  for (int parity = 0; parity < 2; parity++) {
-    uint32_t grid = parity ? p.nregions / 2 : half;
-    if (!grid) continue;
-    if (sparse_max) {
-      const uint32_t sg = (grid + 127) / 128;
-      if (op == Op::kDelete)
-        k_sparse<LOGS, true, false><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
-      else if (cnt)
-        k_sparse<LOGS, false, true><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
-      else
-        k_sparse<LOGS, false, false><<<sg, 128, 0, st>>>(dqf, p, parity, sparse_max, status);
-      count_launch();
-    }
-    if (op == Op::kDelete)
-      k_rebuild<LOGS, true, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, sparse_max, status);
-    else if (cnt)
-      k_rebuild<LOGS, false, true><<<grid, 256, Lay<LOGS, true>::BYTES, st>>>(g, p, parity, sparse_max, status);
-    else
-      k_rebuild<LOGS, false, false><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(g, p, parity, sparse_max, status);
-    count_launch();
-  }
-  return cudaGetLastError();
-}
-
-}  // namespace
 
 size_t rebuild_smem_bytes(int log_region) {
   switch (log_region) {
@@ -719,18 +15,7 @@ size_t rebuild_smem_bytes(int log_region) {
 
 cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_filter* dqf,
                            uint32_t* status, cudaStream_t st, uint32_t sparse_max) {
-  cudaError_t e = cudaMemsetAsync(p.deferred, 0, sizeof(uint32_t), st);
-  if (e != cudaSuccess) return e;
-  switch (p.log_region) {
-    case 11: e = run_phases<11>(g, p, op, dqf, sparse_max, status, st); break;
-    case 12: e = run_phases<12>(g, p, op, dqf, sparse_max, status, st); break;
-    case 13: e = run_phases<13>(g, p, op, dqf, sparse_max, status, st); break;
-    default: return cudaErrorInvalidValue;
-  }
-  if (e != cudaSuccess) return e;
-  k_fallback<<<1, 32, 0, st>>>(dqf, p, op == Op::kDelete ? 1 : 0, status);
-  count_launch();
-  return cudaGetLastError();
+  return run_rebuild(OneFilter{g, dqf}, p, op, status, st, sparse_max);
 }
 
 }  // namespace gqf

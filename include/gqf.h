@@ -194,6 +194,43 @@ int gqf_server_stats(gqf_server* s, double* out, int n);
 int gqf_server_reset_stats(gqf_server* s);
 void gqf_server_destroy(gqf_server* s);
 
+/* ------------------------------------------------------------- filter sets
+ * No counterpart in the reference (one QF handle per filter, one bulk call
+ * sequence per filter).  A set holds n independent filters (filter f has
+ * 2^nbits[f] slots) in one device arena; a batch for all of them is one
+ * array of device keys with device CSR offsets (offsets[0] = 0, filter f
+ * owns keys[offsets[f] .. offsets[f+1]), offsets[n] = total) and runs as one
+ * partition pass, one rebuild launch per parity and one probe launch.  Each
+ * filter's contents, counts and exported bytes equal those of a QF of the
+ * same size given the same keys.  Scratch for max_batch_keys keys is
+ * allocated at creation; the operations allocate nothing and only enqueue
+ * work on `stream`, so they can be captured into a CUDA graph (make one
+ * call of each kind before capturing: the first call configures kernels).
+ *   gqf_set_tune:   times inserts of the given batch under each region size
+ *                   and key-by-key setting, keeps the fastest, and leaves the
+ *                   set empty; *best_ms gets the best time.
+ *   gqf_set_config: region size (11, 12, 13) and key-by-key threshold
+ *                   (as gqf_set_sparse_max; GQF_SPARSE_AUTO by default).
+ *   gqf_set_export: filter i in the reference's packed format (as gqf_export).
+ * Returns 0, or -1 with gqf_last_error set. */
+typedef struct gqf_set gqf_set;
+int gqf_set_create(uint32_t n, const int* nbits, uint64_t max_batch_keys, gqf_set** out);
+void gqf_set_destroy(gqf_set* s);
+int gqf_set_insert(gqf_set* s, const uint64_t* keys, const uint64_t* offsets, uint64_t total, uint8_t flags,
+                   void* stream);
+int gqf_set_delete(gqf_set* s, const uint64_t* keys, const uint64_t* offsets, uint64_t total, uint8_t flags,
+                   void* stream);
+int gqf_set_get(gqf_set* s, const uint64_t* keys, const uint64_t* offsets, uint64_t total, uint64_t* counts,
+                uint8_t flags, void* stream);
+int gqf_set_reset(gqf_set* s, void* stream);
+int gqf_set_tune(gqf_set* s, const uint64_t* keys, const uint64_t* offsets, uint64_t total, uint8_t flags,
+                 double* best_ms);
+int gqf_set_config(gqf_set* s, int log_region, uint32_t sparse_max);
+int gqf_set_get_config(gqf_set* s, int* log_region, uint32_t* sparse_max);
+uint64_t gqf_set_export_size(gqf_set* s, uint32_t i);
+int gqf_set_export(gqf_set* s, uint32_t i, uint8_t* out, uint64_t size);
+int gqf_set_get_status(gqf_set* s, uint32_t* status);
+
 /* The filter's default stream for the reference entry points. */
 int gqf_set_stream(QF* qf, void* stream);
 
