@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-skew", action="store_true", help="skip the skewed-counting workloads")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop workload")
+    ap.add_argument("--no-batched", action="store_true", help="skip the many-filter workload")
     ap.add_argument("--serve-nbits", type=int, default=30)
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="Poisson offered load as a fraction of the measured saturated throughput")
@@ -359,6 +360,10 @@ def run_gpu(args, wl, rank, world):
         del keys, absent, present, out
         torch.cuda.empty_cache()
         workloads["skewed_counting"] = run_skew(args, torch, cqf_gb300)
+    if not args.no_batched and rank == 0 and world == 1:
+        qf.close()
+        torch.cuda.empty_cache()
+        workloads["many_filters"] = run_batched(args, torch, cqf_gb300)
     if not args.no_serve and rank == 0 and world == 1:
         qf.close()
         torch.cuda.empty_cache()
@@ -617,6 +622,116 @@ def run_skew(args, torch, cqf_gb300):
                                     "extracted k-mers")
             del scratch
     del keys, reads, kmers
+    torch.cuda.empty_cache()
+    return res
+
+
+# ------------------------------------------------ many-filter launch (config 4)
+
+def batched_shapes(nfilters=4096, seed=7):
+    """Config 4's filters from splitmix64 seed 7: nbits = 10 + (x >> 32) % 11
+    (uniform in [10, 20]), load = 0.5 + 0.4 u (u a 53-bit uniform of the
+    second stream); filter f gets floor(load * 2^nbits) keys."""
+    from cqf_gb300 import synth
+
+    x = synth.splitmix64(seed, nfilters)
+    u = _u53(synth.splitmix64(seed + 1000, nfilters))
+    nbits = (10 + (x >> np.uint64(32)) % np.uint64(11)).astype(np.int32)
+    loads = 0.5 + 0.4 * u
+    sizes = np.floor(loads * (2.0 ** nbits)).astype(np.int64)
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return nbits, sizes, offsets
+
+
+def run_batched(args, torch, cqf_gb300):
+    """Config 4: 4096 filters filled to their loads in one batch (uniform
+    splitmix64 keys, seed 8) and queried with as many present and absent
+    keys (seed 9).  One step = reset + insert + get present + get absent,
+    captured once as a CUDA graph and replayed; the region size and the
+    key-by-key threshold come from the set's autotuner.  The reference arm
+    runs qf_malloc_device + bulk_insert + bulk_get (present, absent) per
+    filter, one filter after another, as its API requires."""
+    from cqf_gb300 import synth
+
+    nbits, sizes, offsets = batched_shapes()
+    total = int(offsets[-1])
+    keys = synth.splitmix64_dev(8, total)
+    absent = synth.splitmix64_dev(9, total)
+    od = torch.from_numpy(offsets).cuda()
+    cp = torch.empty(total, dtype=torch.int64, device="cuda")
+    ca = torch.empty(total, dtype=torch.int64, device="cuda")
+    fs = cqf_gb300.FilterSet(nbits, total)
+    tune_ms = fs.tune(keys, od)
+    cfg = fs.config()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        fs.reset(stream=s)
+        fs.insert(keys, od, stream=s)
+        fs.get(keys, od, cp, stream=s)
+        fs.get(absent, od, ca, stream=s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        fs.reset(stream=s)
+        fs.insert(keys, od, stream=s)
+        fs.get(keys, od, cp, stream=s)
+        fs.get(absent, od, ca, stream=s)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.steps)
+    e0.record()
+    for _ in range(reps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    found = bool((cp > 0).all().item())
+    fp = int((ca > 0).sum().item())
+    status = fs.status()
+    fs.close()
+    ops = 3 * total
+    res = {
+        "filters": int(nbits.size), "nbits_range": [int(nbits.min()), int(nbits.max())],
+        "keys_inserted": total, "key_ops_per_step": ops,
+        "ms_per_step": round(ms, 3), "mkeys_s": round(ops / ms / 1e3, 1),
+        "graph": "reset + insert + 2 gets captured once, replayed",
+        "autotuned": cfg | {"tune_insert_ms": round(tune_ms, 3)},
+        "present_all_found": found, "false_positives": fp, "status": status,
+    }
+    if not args.no_ref_cuda:
+        from oracle import refgpu
+
+        if refgpu.available():
+            out = torch.empty(int(sizes.max()), dtype=torch.int64, device="cuda")
+            scratch = torch.empty(int(sizes.max()), dtype=torch.int64, device="cuda")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ok = True
+            sample = range(0, nbits.size, 16)  # every 16th filter: the same size law
+            for f in sample:
+                a, n = int(offsets[f]), int(sizes[f])
+                r = refgpu.RefGPU(int(nbits[f]))
+                scratch[:n].copy_(keys[a:a + n])
+                r.bulk_insert(scratch, n)
+                r.bulk_get(keys[a:a + n], out, n)
+                if f % 256 == 0:
+                    ok &= bool((out[:n] > 0).all().item())
+                r.bulk_get(absent[a:a + n], out, n)
+                r.close()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            sops = 3 * int(sum(int(sizes[f]) for f in sample))
+            rate = sops / dt / 1e6
+            res["ref_cuda"] = {"sample_seconds": round(dt, 3), "sample_filters": len(sample), "mkeys_s": round(rate, 1),
+                               "seconds_all_filters_est": round(ops / rate / 1e6, 1),
+                               "present_found_sampled": ok,
+                               "what": "per filter: device buffers + bulk_insert + bulk_get x2 of the reference's "
+                                       "kernels (oracle/refgpu.py), synchronised as its API is; every 16th "
+                                       "filter timed, rate over the sample's key operations"}
+            res["speedup_vs_ref_cuda"] = round((ops / ms / 1e3) / rate, 1)
+    del keys, absent, cp, ca
     torch.cuda.empty_cache()
     return res
 

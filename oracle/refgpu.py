@@ -67,8 +67,35 @@ class _Driver:
             raise RuntimeError(f"{what}: CUDA driver error {rc}")
 
 
+_MODULE = {}  # the driver library, the loaded cubin and its kernels, once per process
+
+
+def _driver():
+    if "driver" not in _MODULE:
+        _MODULE["driver"] = _Driver()
+    return _MODULE["driver"]
+
+
+def _module(d):
+    if "mod" not in _MODULE:
+        # per-thread stack of this process's context: the counted insert's
+        # frames (1120 bytes, all static) fit with a wide margin
+        d.check(d.cu.cuCtxSetLimit(CU_LIMIT_STACK_SIZE, 8192), "cuCtxSetLimit")
+        mod = ctypes.c_void_p()
+        d.check(d.cu.cuModuleLoad(ctypes.byref(mod), CUBIN.encode()), "cuModuleLoad")
+        fn = {}
+        for k, name in KERNELS.items():
+            f = ctypes.c_void_p()
+            d.check(d.cu.cuModuleGetFunction(ctypes.byref(f), mod, name.encode()), name)
+            fn[k] = f
+        _MODULE["mod"], _MODULE["fn"] = mod, fn
+    return _MODULE["fn"]
+
+
 class RefGPU:
-    """One filter of the reference's CUDA build (2^nbits slots)."""
+    """One filter of the reference's CUDA build (2^nbits slots).  The cubin
+    is loaded once per process and kept; a filter costs only its device
+    buffers, as a qf_malloc_device does."""
 
     def __init__(self, nbits: int):
         import torch
@@ -78,19 +105,10 @@ class RefGPU:
         self.torch = torch
         torch.cuda.init()
         torch.zeros(1, device="cuda")  # primary context current on this thread
-        self.d = _Driver()
+        self.d = _driver()
         with open(LAYOUT) as fh:
             self.lay = json.load(fh)
-        # per-thread stack of this process's context: the counted insert's
-        # frames (1120 bytes, all static) fit with a wide margin
-        self.d.check(self.d.cu.cuCtxSetLimit(CU_LIMIT_STACK_SIZE, 8192), "cuCtxSetLimit")
-        self.mod = ctypes.c_void_p()
-        self.d.check(self.d.cu.cuModuleLoad(ctypes.byref(self.mod), CUBIN.encode()), "cuModuleLoad")
-        self.fn = {}
-        for k, name in KERNELS.items():
-            f = ctypes.c_void_p()
-            self.d.check(self.d.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
-            self.fn[k] = f
+        self.fn = _module(self.d)
         # qf_init sizing (src/gqf.cu:1939-1996) for qf_malloc_device's parameters
         self.nbits = nbits
         self.nslots = 1 << nbits
@@ -125,10 +143,11 @@ class RefGPU:
         torch.cuda.synchronize()
 
     def close(self):
-        if getattr(self, "mod", None) and self.mod.value:
+        """Releases the filter's buffers (after its queued work)."""
+        if getattr(self, "blocks", None) is not None:
             self.torch.cuda.synchronize()
-            self.d.cu.cuModuleUnload(self.mod)
-            self.mod = None
+            self.blocks = self.meta = self.locks = self.buffers = self.buffer_sizes = None
+            self.runtime = self.qf = None
 
     def _launch(self, name, grid, block, *args):
         holders = []
