@@ -59,6 +59,11 @@ SIGNATURES = {
     "gqf_bulk_insert_noalloc": (_int, [_vp, _u64, _vp, _u8, _vp]),
     "gqf_bulk_insert_kmers": (_int, [_vp, _vp, _u64, _u32, _u32, _vp]),
     "gqf_kmers_extract": (_int, [_vp, _u64, _u32, _u32, _vp, _vp]),
+    "gqf_enumerate": (_int, [_vp, _vp, _vp, _u64, ctypes.POINTER(_u64), _int]),
+    "gqf_merge": (_int, [_vp, _vp, _vp]),
+    "gqf_multi_merge": (_int, [_vp, _int, _vp]),
+    "gqf_intersect": (_int, [_vp, _vp, _vp]),
+    "gqf_inner_product": (_u64, [_vp, _vp]),
     "gqf_set_create": (_int, [_u32, _vp, _u64, ctypes.POINTER(_vp)]),
     "gqf_set_destroy": (None, [_vp]),
     "gqf_set_insert": (_int, [_vp, _vp, _vp, _u64, _u8, _vp]),
@@ -293,6 +298,30 @@ class QF:
 
     def reset(self):
         self._ok(self.L.gqf_reset(self.h))
+
+    def enumerate(self, as_keys: bool = False):
+        """(hashes, counts) as host uint64 arrays, in increasing hash order."""
+        import torch
+
+        n = _u64(0)
+        self._ok(self.L.gqf_enumerate(self.h, 0, 0, 0, ctypes.byref(n), 0))
+        m = max(1, n.value)
+        h = torch.empty(m, dtype=torch.int64, device="cuda")
+        c = torch.empty(m, dtype=torch.int64, device="cuda")
+        self._ok(self.L.gqf_enumerate(self.h, h.data_ptr(), c.data_ptr(), m, ctypes.byref(n), int(as_keys)))
+        k = n.value
+        return h[:k].cpu().numpy().view(np.uint64), c[:k].cpu().numpy().view(np.uint64)
+
+    def merge_from(self, *others: "QF"):
+        """Inserts every (hash, count) of the other filters (gqf_multi_merge)."""
+        arr = (_vp * len(others))(*[o.h for o in others])
+        self._ok(self.L.gqf_multi_merge(arr, len(others), self.h))
+
+    def intersect_from(self, a: "QF", b: "QF"):
+        self._ok(self.L.gqf_intersect(a.h, b.h, self.h))
+
+    def inner_product(self, other: "QF") -> int:
+        return int(self.L.gqf_inner_product(self.h, other.h))
 
     def export(self) -> np.ndarray:
         n = int(self.L.gqf_export_size(self.h))

@@ -692,6 +692,234 @@ int gqf_profile_read(QF* qf, double* ms, uint64_t* calls, uint64_t* keys) {
   return 0;
 }
 
+
+// ------------------------------------------------------------- enumeration
+
+namespace {
+
+// Counts f's pairs per block and scans them into *start (device, allocated
+// here on `st`; the caller frees it).  Returns the total, or UINT64_MAX.
+uint64_t enum_prepare(HostFilter* f, cudaStream_t st, uint32_t** start) {
+  const uint64_t nb = f->h.nblocks;
+  *start = nullptr;
+  if (64 * nb >= (1ULL << 32)) {
+    set_err("enumeration supports tables of at most 2^31 slots");
+    return UINT64_MAX;
+  }
+  uint32_t* buf = nullptr;  // cnt[nb] | start[nb + 1] | cursor[nb] | scan scratch
+  const uint64_t words = 3 * nb + 1 + nb / 4096 + 4;
+  if (!ck(cudaMallocAsync((void**)&buf, words * sizeof(uint32_t), st), "cudaMallocAsync")) return UINT64_MAX;
+  Partition tp{};
+  tp.region_count = buf;
+  tp.region_start = buf + nb;
+  tp.cursor = buf + 2 * nb + 1;
+  tp.deferred = buf + 3 * nb + 1;
+  tp.nregions = (uint32_t)nb;
+  uint32_t total = 0;
+  if (!ck(launch_enum_count(f->g, tp.region_count, st), "enumerate") || !ck(launch_region_scan(tp, st), "scan") ||
+      !ck(cudaMemcpyAsync(&total, tp.region_start + nb, 4, cudaMemcpyDeviceToHost, st), "memcpy") ||
+      !ck(cudaStreamSynchronize(st), "sync")) {
+    cudaFreeAsync(buf, st);
+    return UINT64_MAX;
+  }
+  *start = buf;  // the counts come first; the starts follow at buf + nb
+  return total;
+}
+
+// Inserts (hash, count) pairs into f with the counted rebuild.
+int insert_pairs(HostFilter* f, const uint64_t* h, const uint32_t* c, uint64_t n, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(f->mu);
+  if (n == 0) return 0;
+  if (!ensure_partition(f, n, true, st)) return -1;
+  Partition p = f->part;
+  if (!ck(launch_partition_counted(f->g, p, h, c, n, nullptr, 1, status_ptr(f), st), "partition") ||
+      !ck(launch_merge_regions(p, st), "merge_regions") ||
+      !ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st, sparse_max_for(f, n)), "rebuild"))
+    return -1;
+  return 0;
+}
+
+// The pairs of several filters, concatenated, as hashes and uint32 counts in
+// one device allocation (freed by the caller); *n gets the total.
+bool collect_pairs(std::vector<HostFilter*> fs, cudaStream_t st, uint64_t** h, uint32_t** c, uint64_t* n) {
+  std::vector<uint32_t*> starts;
+  std::vector<uint64_t> counts;
+  uint64_t total = 0;
+  bool good = true;
+  for (HostFilter* f : fs) {
+    uint32_t* st_buf = nullptr;
+    const uint64_t k = enum_prepare(f, st, &st_buf);
+    if (k == UINT64_MAX) {
+      good = false;
+      break;
+    }
+    starts.push_back(st_buf);
+    counts.push_back(k);
+    total += k;
+  }
+  *h = nullptr;
+  *c = nullptr;
+  uint32_t* flag = nullptr;
+  if (good)
+    good = ck(cudaMallocAsync((void**)h, (total ? total : 1) * 8, st), "cudaMallocAsync") &&
+           ck(cudaMallocAsync((void**)c, (total ? total : 1) * 4, st), "cudaMallocAsync") &&
+           ck(cudaMallocAsync((void**)&flag, 4, st), "cudaMallocAsync") && ck(cudaMemsetAsync(flag, 0, 4, st), "memset");
+  uint64_t at = 0;
+  for (size_t i = 0; good && i < starts.size(); i++) {
+    good = ck(launch_enum_write(fs[i]->g, starts[i] + fs[i]->h.nblocks, 0, *h + at, nullptr, *c + at, flag, st),
+              "enumerate");
+    at += counts[i];
+  }
+  uint32_t over = 0;
+  if (good)
+    good = ck(cudaMemcpyAsync(&over, flag, 4, cudaMemcpyDeviceToHost, st), "memcpy") &&
+           ck(cudaStreamSynchronize(st), "sync");
+  if (good && over) {
+    set_err("a counter above 2^32 - 1 cannot be carried by this operation");
+    good = false;
+  }
+  for (uint32_t* b : starts) cudaFreeAsync(b, st);
+  if (flag) cudaFreeAsync(flag, st);
+  if (!good) {
+    if (*h) cudaFreeAsync(*h, st);
+    if (*c) cudaFreeAsync(*c, st);
+    *h = nullptr;
+    *c = nullptr;
+    return false;
+  }
+  *n = total;
+  return true;
+}
+
+// The reference iterates the larger filter and probes the smaller
+// (qf_inner_product / qf_intersect, src/gqf.cu:4010-4080): "larger" by table
+// bytes, ties to the second filter.
+void disk_and_mem(HostFilter* a, HostFilter* b, HostFilter** disk, HostFilter** mem) {
+  if (a->h.nblocks > b->h.nblocks) {
+    *disk = a;
+    *mem = b;
+  } else {
+    *disk = b;
+    *mem = a;
+  }
+}
+
+}  // namespace
+
+int gqf_enumerate(QF* qf, uint64_t* hashes, uint64_t* counts, uint64_t cap, uint64_t* n, int as_keys) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  cudaStream_t st = 0;
+  uint32_t* buf = nullptr;
+  const uint64_t total = enum_prepare(f, st, &buf);
+  if (total == UINT64_MAX) return -1;
+  if (n) *n = total;
+  int rc = 0;
+  if (hashes) {
+    if (total > cap) {
+      set_err("gqf_enumerate: output holds fewer pairs than the filter has (see *n)");
+      rc = -1;
+    } else if (!ck(launch_enum_write(f->g, buf + f->h.nblocks, as_keys, hashes, counts, nullptr, nullptr, st),
+                   "enumerate") || !ck(cudaStreamSynchronize(st), "sync")) {
+      rc = -1;
+    }
+  }
+  cudaFreeAsync(buf, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+int gqf_multi_merge(QF* const* in, int nin, QF* out) {
+  HostFilter* r = lookup(out);
+  if (!r || nin < 0 || (nin && !in)) return -1;
+  std::vector<HostFilter*> fs;
+  for (int i = 0; i < nin; i++) {
+    HostFilter* f = lookup(in[i]);
+    if (!f) return -1;
+    fs.push_back(f);
+  }
+  cudaStream_t st = 0;
+  uint64_t* h = nullptr;
+  uint32_t* c = nullptr;
+  uint64_t n = 0;
+  if (!collect_pairs(fs, st, &h, &c, &n)) return -1;  // every input read before the output changes
+  const int rc = insert_pairs(r, h, c, n, st);
+  cudaFreeAsync(h, st);
+  cudaFreeAsync(c, st);
+  return ck(cudaStreamSynchronize(st), "sync") ? rc : -1;
+}
+
+int gqf_merge(QF* a, QF* b, QF* out) {
+  QF* in[2] = {a, b};
+  return gqf_multi_merge(in, 2, out);
+}
+
+int gqf_intersect(QF* a, QF* b, QF* out) {
+  HostFilter *fa = lookup(a), *fb = lookup(b), *fr = lookup(out);
+  if (!fa || !fb || !fr) return -1;
+  HostFilter *disk, *mem;
+  disk_and_mem(fa, fb, &disk, &mem);
+  cudaStream_t st = 0;
+  uint32_t* buf = nullptr;
+  const uint64_t total = enum_prepare(disk, st, &buf);
+  if (total == UINT64_MAX) return -1;
+  uint64_t *h = nullptr, *cc = nullptr, *kh = nullptr;
+  uint32_t *kc = nullptr, *flag = nullptr;
+  unsigned long long* nk = nullptr;
+  unsigned long long kept = 0;
+  uint32_t over = 0;
+  const uint64_t m = total ? total : 1;
+  bool good = ck(cudaMallocAsync((void**)&h, m * 8, st), "cudaMallocAsync") &&
+              ck(cudaMallocAsync((void**)&cc, m * 8, st), "cudaMallocAsync") &&
+              ck(cudaMallocAsync((void**)&kh, m * 8, st), "cudaMallocAsync") &&
+              ck(cudaMallocAsync((void**)&kc, m * 4, st), "cudaMallocAsync") &&
+              ck(cudaMallocAsync((void**)&flag, 16, st), "cudaMallocAsync") &&
+              ck(cudaMemsetAsync(flag, 0, 16, st), "memset");
+  nk = reinterpret_cast<unsigned long long*>(flag + 2);
+  good = good && ck(launch_enum_write(disk->g, buf + disk->h.nblocks, 0, h, cc, nullptr, nullptr, st), "enumerate") &&
+         ck(launch_pair_probe(mem->g, h, cc, total, nullptr, kh, kc, nk, flag, st), "probe") &&
+         ck(cudaMemcpyAsync(&kept, nk, 8, cudaMemcpyDeviceToHost, st), "memcpy") &&
+         ck(cudaMemcpyAsync(&over, flag, 4, cudaMemcpyDeviceToHost, st), "memcpy") &&
+         ck(cudaStreamSynchronize(st), "sync");
+  if (good && over) {
+    set_err("a counter above 2^32 - 1 cannot be carried by this operation");
+    good = false;
+  }
+  int rc = good ? insert_pairs(fr, kh, kc, kept, st) : -1;
+  for (void* p : {(void*)buf, (void*)h, (void*)cc, (void*)kh, (void*)kc, (void*)flag})
+    if (p) cudaFreeAsync(p, st);
+  if (!ck(cudaStreamSynchronize(st), "sync")) rc = -1;
+  return rc;
+}
+
+uint64_t gqf_inner_product(QF* a, QF* b) {
+  HostFilter *fa = lookup(a), *fb = lookup(b);
+  if (!fa || !fb) return 0;
+  HostFilter *disk, *mem;
+  disk_and_mem(fa, fb, &disk, &mem);
+  cudaStream_t st = 0;
+  uint32_t* buf = nullptr;
+  const uint64_t total = enum_prepare(disk, st, &buf);
+  if (total == UINT64_MAX) return 0;
+  uint64_t *h = nullptr, *cc = nullptr;
+  unsigned long long* acc = nullptr;
+  unsigned long long out = 0;
+  const uint64_t m = total ? total : 1;
+  const bool good = ck(cudaMallocAsync((void**)&h, m * 8, st), "cudaMallocAsync") &&
+                    ck(cudaMallocAsync((void**)&cc, m * 8, st), "cudaMallocAsync") &&
+                    ck(cudaMallocAsync((void**)&acc, 8, st), "cudaMallocAsync") &&
+                    ck(cudaMemsetAsync(acc, 0, 8, st), "memset") &&
+                    ck(launch_enum_write(disk->g, buf + disk->h.nblocks, 0, h, cc, nullptr, nullptr, st),
+                       "enumerate") &&
+                    ck(launch_pair_probe(mem->g, h, cc, total, acc, nullptr, nullptr, nullptr, nullptr, st), "probe") &&
+                    ck(cudaMemcpyAsync(&out, acc, 8, cudaMemcpyDeviceToHost, st), "memcpy") &&
+                    ck(cudaStreamSynchronize(st), "sync");
+  for (void* p : {(void*)buf, (void*)h, (void*)cc, (void*)acc})
+    if (p) cudaFreeAsync(p, st);
+  cudaStreamSynchronize(st);
+  return good ? (uint64_t)out : 0;
+}
+
 uint64_t gqf_launch_count(void) { return g_launches.load(); }
 
 int gqf_debug_serial_apply(QF* qf, const uint64_t* hashes, uint64_t n, int op) {

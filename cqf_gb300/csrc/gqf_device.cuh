@@ -87,6 +87,30 @@ GQF_HD uint64_t hash64(uint64_t key, uint64_t mask) {
   return key;
 }
 
+// hash_64i (src/hashutil.cu:146-170): the inverse of hash64 under the same
+// mask, undoing its steps in reverse order (used to report keys, as the
+// reference's qfi_get_key does for invertible filters).
+GQF_HD uint64_t hash64i(uint64_t key, uint64_t mask) {
+  uint64_t tmp;
+  tmp = key - (key << 31);  // invert key + (key << 31)
+  key = (key - (tmp << 31)) & mask;
+  tmp = key ^ key >> 28;  // invert key ^ key >> 28
+  key = key ^ tmp >> 28;
+  key = (key * 14933078535860113213ull) & mask;  // inverse of 21 mod 2^64
+  tmp = key ^ key >> 14;  // invert key ^ key >> 14
+  tmp = key ^ tmp >> 14;
+  tmp = key ^ tmp >> 14;
+  key = key ^ tmp >> 14;
+  key = (key * 15244667743933553977ull) & mask;  // inverse of 265 mod 2^64
+  tmp = key ^ key >> 24;  // invert key ^ key >> 24
+  key = key ^ tmp >> 24;
+  tmp = ~key;  // invert ~key + (key << 21)
+  tmp = ~(key - (tmp << 21));
+  tmp = ~(key - (tmp << 21));
+  key = ~(key - (tmp << 21)) & mask;
+  return key;
+}
+
 GQF_HD int popc64(uint64_t v) {
 #ifdef __CUDA_ARCH__
   return __popcll(v);

@@ -151,6 +151,17 @@ cudaError_t launch_rebuild(const Geom& g, const Partition& p, Op op, quotient_fi
                            uint32_t* status, cudaStream_t st, uint32_t sparse_max = kDefaultSparseMax);
 size_t rebuild_smem_bytes(int log_region);
 
+// Enumeration (gqf_iter.cu): pairs per block, then the pairs themselves at
+// start[b] (an exclusive scan of the per-block numbers) in hash order.
+cudaError_t launch_enum_count(const Geom& g, uint32_t* per_block, cudaStream_t st);
+cudaError_t launch_enum_write(const Geom& g, const uint32_t* start, int as_keys, uint64_t* out_h, uint64_t* out_c,
+                              uint32_t* out_c32, uint32_t* overflow, cudaStream_t st);
+// Probes `mem` for n (hash, count) pairs: *acc += count * count in mem, and/or
+// the pairs present in mem appended at out_*[*n_out].
+cudaError_t launch_pair_probe(const Geom& mem, const uint64_t* h, const uint64_t* c, uint64_t n,
+                              unsigned long long* acc, uint64_t* out_h, uint32_t* out_c32,
+                              unsigned long long* n_out, uint32_t* overflow, cudaStream_t st);
+
 cudaError_t launch_export(const Geom& g, uint8_t* packed, cudaStream_t st);
 cudaError_t launch_import(const Geom& g, const uint8_t* packed, cudaStream_t st);
 cudaError_t launch_import_fix(quotient_filter* dqf, const uint8_t* packed, cudaStream_t st);

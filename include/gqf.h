@@ -194,6 +194,30 @@ int gqf_server_stats(gqf_server* s, double* out, int n);
 int gqf_server_reset_stats(gqf_server* s);
 void gqf_server_destroy(gqf_server* s);
 
+/* ---------------------------------------------- enumeration and set algebra
+ * The reference's iterator and the operations built on it, run on the GPU
+ * (host-only in the reference: qfi_get_hash / qfi_get_key / qfi_next,
+ * src/gqf.cu:3774-3893; qf_merge :3896; qf_multi_merge :3945;
+ * qf_inner_product :4010; qf_intersect :4047).  All take device filters,
+ * synchronise, and leave their inputs unchanged.
+ *   gqf_enumerate: every (hash, count) in increasing hash order, the
+ *     iterator's order, into device arrays of `cap` entries (counts may be
+ *     NULL); *n gets the number of pairs.  hashes = NULL only counts them.
+ *     as_keys reports keys (the inverse hash, as qfi_get_key does for the
+ *     invertible hash) instead of hashes.  Tables up to 2^31 slots.
+ *   gqf_merge / gqf_multi_merge: inserts every pair of the inputs into `out`
+ *     (as hashes, like the reference); `out` may be one of the inputs.
+ *   gqf_intersect: the pairs of the larger input (by table size, ties to b)
+ *     whose hash the other input holds, inserted into `out`.
+ *   gqf_inner_product: sum over the larger input's pairs of count times the
+ *     other input's count of the same hash (0 on error).
+ * Counters above 2^32 - 1 cannot be carried into `out` (-1). */
+int gqf_enumerate(QF* qf, uint64_t* hashes, uint64_t* counts, uint64_t cap, uint64_t* n, int as_keys);
+int gqf_merge(QF* a, QF* b, QF* out);
+int gqf_multi_merge(QF* const* in, int nin, QF* out);
+int gqf_intersect(QF* a, QF* b, QF* out);
+uint64_t gqf_inner_product(QF* a, QF* b);
+
 /* ------------------------------------------------------------- filter sets
  * No counterpart in the reference (one QF handle per filter, one bulk call
  * sequence per filter).  A set holds n independent filters (filter f has
