@@ -287,28 +287,84 @@ struct Serial {
     }
   }
 
+  // Slots as aligned 8-byte words: word k holds slots 8k .. 8k+7 (byte j of
+  // the word is slot 8k + j).  A block's slots start 32 bytes into it, so
+  // every such word is 8-byte aligned.
+  GQF_HDF unsigned long long& slot_word(uint64_t k) const {
+    return reinterpret_cast<unsigned long long*>(b[k >> 3].slots)[k & 7];
+  }
+  // The 8 slots starting at slot i (any alignment; i + 8 <= 64 * nblocks).
+  GQF_HDF unsigned long long slots8(uint64_t i) const {
+    const uint64_t k = i >> 3;
+    const int sh = (int)(i & 7) * 8;
+    const unsigned long long lo = slot_word(k);
+    if (!sh) return lo;
+    return (lo >> sh) | (slot_word(k + 1) << (64 - sh));
+  }
+
+  // shift_slots (src/gqf.cu:973): slots [first, last] move up by distance.
+  // Whole aligned destination words at a time, highest first (a destination
+  // word's sources all lie below it); bytes outside the destination range
+  // keep their values.
+  GQF_HDF void shift_slots(uint64_t first, uint64_t last, uint64_t distance) const {
+    if (last + 1 <= first) return;
+    const uint64_t dlo = first + distance, dhi = last + distance;
+    if (distance == 0 || dhi >= 64 * nblocks) {  // (a full table) the byte loop stops at the end
+      for (uint64_t i = last + 1; i-- > first;) set_slot(i + distance, get_slot(i));
+      return;
+    }
+    for (uint64_t k = dhi >> 3;; k--) {
+      const uint64_t ws = 8 * k;
+      const uint64_t lo = ws > dlo ? ws : dlo, hi = ws + 7 < dhi ? ws + 7 : dhi;
+      unsigned long long mask = 0;
+      for (uint64_t j = lo; j <= hi; j++) mask |= 0xFFULL << (8 * (j - ws));
+      unsigned long long src;
+      if (ws >= distance) {
+        src = slots8(ws - distance);
+      } else {  // the word's lowest bytes have no source: only [lo, hi] matters
+        src = 0;
+        for (uint64_t j = lo; j <= hi; j++) src |= (unsigned long long)get_slot(j - distance) << (8 * (j - ws));
+      }
+      unsigned long long& w = slot_word(k);
+      w = (w & ~mask) | (src & mask);
+      if (ws <= dlo) break;
+    }
+  }
+
   // shift_remainders (src/gqf.cu:897-937): slots [start, empty) move up one.
   GQF_HDF void shift_remainders(uint64_t start, uint64_t empty) const {
-    for (uint64_t i = empty; i > start; i--) set_slot(i, get_slot(i - 1));
+    if (empty > start) shift_slots(start, empty - 1, 1);
   }
 
   // shift_runends (src/gqf.cu:984-1011): runend bits of [first, last] move up
   // by distance; bits in [first, first+distance) are cleared.  last may be
   // first - 1 (an empty range), which only clears, as the reference does.
+  // Whole runends words at a time, highest first.
   GQF_HDF void shift_runends(uint64_t first, uint64_t last, uint64_t distance) const {
-    for (uint64_t i = last + 1; i-- > first;) {
-      uint64_t d = i + distance;
-      unsigned long long bit = (run_word(i) >> (i % 64)) & 1ULL;
-      run_word(d) = (run_word(d) & ~(1ULL << (d % 64))) | (bit << (d % 64));
+    if (last + 1 > first) {
+      const uint64_t dlo = first + distance, dhi = last + distance;
+      if (distance == 0 || distance >= 64 || dhi >= 64 * nblocks) {
+        for (uint64_t i = last + 1; i-- > first;) {
+          uint64_t d = i + distance;
+          unsigned long long bit = (run_word(i) >> (i % 64)) & 1ULL;
+          run_word(d) = (run_word(d) & ~(1ULL << (d % 64))) | (bit << (d % 64));
+        }
+      } else {
+        for (uint64_t k = dhi >> 6;; k--) {
+          const uint64_t ws = 64 * k;
+          const uint64_t lo = ws > dlo ? ws : dlo, hi = ws + 63 < dhi ? ws + 63 : dhi;
+          const unsigned long long mask = (hi - ws == 63 ? ~0ULL : ((2ULL << (hi - ws)) - 1ULL)) &
+                                          ~((1ULL << (lo - ws)) - 1ULL);
+          const unsigned long long cur = b[k].runends;
+          const unsigned long long prev = k ? b[k - 1].runends : 0ULL;  // still unmoved
+          const unsigned long long src = (cur << distance) | (prev >> (64 - distance));
+          b[k].runends = (cur & ~mask) | (src & mask);
+          if (ws <= dlo) break;
+        }
+      }
     }
-    for (uint64_t i = first; i < first + distance && i <= last + distance; i++)
-      run_word(i) &= ~(1ULL << (i % 64));
-  }
-
-  // shift_slots (src/gqf.cu:973)
-  GQF_HDF void shift_slots(uint64_t first, uint64_t last, uint64_t distance) const {
-    if (last + 1 <= first) return;
-    for (uint64_t i = last + 1; i-- > first;) set_slot(i + distance, get_slot(i));
+    const uint64_t cend = first + distance - 1 < last + distance ? first + distance - 1 : last + distance;
+    for (uint64_t i = first; i <= cend && distance; i++) run_word(i) &= ~(1ULL << (i % 64));
   }
 
   // find_next_n_empty_slots (src/gqf.cu:964)

@@ -26,6 +26,8 @@
 // reference's own single-key algorithms (gqf_device.cuh), which handles any
 // cluster length and reports a full table like the reference does.
 #pragma once
+#include <algorithm>
+
 #include "gqf_kernels.cuh"
 
 namespace gqf {
@@ -74,9 +76,10 @@ struct Lay {
 };
 
 constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
-// cursor[r] value by which k_sparse hands region r to k_rebuild (the cursors
-// are free once the partition has scattered the keys)
-constexpr uint32_t kHandOff = 0xFFFFFFFFu;
+// The work list of one phase lives in the partition's cursor array (free once
+// the keys are scattered): [0] regions listed by k_sparse, [1] the next one
+// a rebuild CTA takes, [2 ...] the region indices.
+constexpr int kListCount = 0, kListNext = 1, kListBase = 2;
 
 // ----------------------------------------------------- shared-memory image
 
@@ -211,22 +214,18 @@ __device__ int scan_sum(int v, int* tmp, int* total) {
 
 // CNT: the batch carries a multiplicity per key (p.counts), as produced by
 // the duplicate-merging pass of bulk_insert_reduce.
+// Rebuilds region R of the launch (all threads of the CTA).
 template <int LOGS, bool DEL, bool CNT, class Loc>
-__global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
-                                                                             uint32_t sparse_max,
-                                                                             uint32_t* status) {
+__device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& p, const uint32_t R,
+                                               uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
   extern __shared__ __align__(128) uint8_t sm[];
   __shared__ int s_i[8];
   __shared__ int sa[32], sb[32];
 
-  const uint32_t R = 2 * blockIdx.x + parity;  // the launch's region index
-  if (R >= p.nregions) return;
   const uint32_t kbeg = p.region_start[R], kend = kbeg + p.region_count[R];
   if (kbeg == kend) return;
-  // regions up to sparse_max keys belong to k_sparse, unless it handed them on
-  if (kend - kbeg <= sparse_max && p.cursor[R] != kHandOff) return;
   Geom g;
   uint32_t r;  // the region within its filter
   const quotient_filter* dq;
@@ -592,6 +591,30 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc 
   }
 }
 
+// The rebuild of one phase.  With a work list (key-by-key updates on): a
+// persistent grid whose CTAs take the regions k_sparse listed, one at a
+// time, until the list is exhausted.  Without: one CTA per region of the
+// parity, in region order.
+template <int LOGS, bool DEL, bool CNT, class Loc>
+__global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
+                                                                             int use_list, uint32_t* status) {
+  if (!use_list) {
+    const uint32_t R = 2 * blockIdx.x + parity;
+    if (R < p.nregions) rebuild_region<LOGS, DEL, CNT>(loc, p, R, status);
+    return;
+  }
+  __shared__ uint32_t s_take;
+  const uint32_t count = p.cursor[kListCount];
+  for (;;) {
+    __syncthreads();  // the previous region is written back before its memory is reused
+    if (threadIdx.x == 0) s_take = atomicAdd(&p.cursor[kListNext], 1u);
+    __syncthreads();
+    const uint32_t i = s_take;
+    if (i >= count) return;
+    rebuild_region<LOGS, DEL, CNT>(loc, p, p.cursor[kListBase + i], status);
+  }
+}
+
 // Sparse regions.  The rebuild visits every quotient and slot of its window
 // whatever the number of keys, so a region holding only a few keys (a small
 // batch, or a large table) is cheaper to update key by key: one thread per
@@ -602,33 +625,45 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc 
 //
 // Before writing anything the thread proves (Serial::sparse_fits) that the
 // region's changes stay inside the window a rebuild would own, [base, base +
-// REG + PUSH); otherwise it leaves the region untouched to the rebuild that
-// follows in the same phase.
+// REG + PUSH); otherwise it lists the region, untouched, for the rebuild that
+// follows in the same phase, as it lists every region with more keys.
 template <int LOGS, bool DEL, bool CNT, class Loc>
 __global__ void __launch_bounds__(128) k_sparse(Loc loc, Partition p, int parity, uint32_t sparse_max,
                                                 uint32_t* status) {
   const uint32_t R = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + parity;
-  if (R >= p.nregions) return;
-  const uint32_t cnt = p.region_count[R];
-  if (cnt == 0 || cnt > sparse_max) return;
+  const uint32_t cnt = R < p.nregions ? p.region_count[R] : 0;
   Geom g;
-  uint32_t r;
-  const quotient_filter* dq;
-  if (!loc.locate(R, LOGS, &g, &r, &dq)) return;
+  uint32_t r = 0;
+  const quotient_filter* dq = nullptr;
+  const bool real = cnt && loc.locate(R, LOGS, &g, &r, &dq);
+  bool listed = real && cnt > sparse_max;
+  bool mine = real && !listed;
+  uint64_t grow = 0;  // slots the batch may add (0 for deletes)
+  if (mine && !DEL)
+    for (uint32_t k = p.region_start[R]; k < p.region_start[R] + cnt; k++)
+      grow += Serial::insert_growth(CNT ? p.counts[k] : 1);
+  if (mine) {
+    const Serial S(dq);
+    const uint64_t base = (uint64_t)r << LOGS;
+    // a block boundary at or below nslots (a filter smaller than a region is
+    // one region)
+    const uint64_t region_end = min((uint64_t)(base + (1ULL << LOGS)), (uint64_t)S.nslots);
+    const uint64_t bound = min(base + (uint64_t)Lay<LOGS, false>::WIN, min(S.xnslots, 64 * S.nblocks));
+    if (!S.sparse_fits(region_end, grow, bound)) {
+      listed = true;
+      mine = false;
+    }
+  }
+  // append the listed regions (one atomic per warp)
+  const unsigned want = __ballot_sync(0xffffffffu, listed);
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t at = 0;
+  if (lane == 0 && want) at = atomicAdd(&p.cursor[kListCount], (uint32_t)__popc(want));
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if (listed) p.cursor[kListBase + at + __popc(want & ((1u << lane) - 1u))] = R;
+  if (!mine) return;
   const Serial S(dq);
   const uint32_t kbeg = p.region_start[R];
-  const uint64_t base = (uint64_t)r << LOGS;
-  // a block boundary at or below nslots (a filter smaller than a region is
-  // one region)
-  const uint64_t region_end = min((uint64_t)(base + (1ULL << LOGS)), (uint64_t)S.nslots);
-  const uint64_t bound = min(base + (uint64_t)Lay<LOGS, false>::WIN, min(S.xnslots, 64 * S.nblocks));
-  uint64_t grow = 0;  // slots the batch may add (0 for deletes)
-  if (!DEL)
-    for (uint32_t k = kbeg; k < kbeg + cnt; k++) grow += Serial::insert_growth(CNT ? p.counts[k] : 1);
-  if (!S.sparse_fits(region_end, grow, bound)) {
-    p.cursor[R] = kHandOff;
-    return;
-  }
   const int shift = 8 + LOGS;
   for (uint32_t k = kbeg; k < kbeg + cnt; k++) {
     const uint64_t h = ((uint64_t)r << shift) | p.keys[k];
@@ -689,6 +724,20 @@ void configure() {
   done = true;
 }
 
+// CTAs of k_rebuild resident at once on the device.
+template <int LOGS, bool DEL, bool CNT, class Loc>
+uint32_t resident() {
+  static uint32_t n = 0;  // per instantiation
+  if (!n) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild<LOGS, DEL, CNT, Loc>, 256, Lay<LOGS, CNT>::BYTES);
+    n = (uint32_t)std::max(1, sms) * (uint32_t)std::max(1, per);
+  }
+  return n;
+}
+
 template <int LOGS, class Loc>
 cudaError_t run_phases(const Loc& loc, const Partition& p, Op op, uint32_t sparse_max, uint32_t* status,
                        cudaStream_t st) {
@@ -701,7 +750,10 @@ cudaError_t run_phases(const Loc& loc, const Partition& p, Op op, uint32_t spars
   for (int parity = 0; parity < 2; parity++) {
     uint32_t grid = parity ? p.nregions / 2 : half;
     if (!grid) continue;
-    if (sparse_max) {
+    const int use_list = sparse_max != 0;
+    if (use_list) {
+      cudaError_t e = cudaMemsetAsync(p.cursor, 0, 2 * sizeof(uint32_t), st);
+      if (e != cudaSuccess) return e;
       const uint32_t sg = (grid + 127) / 128;
       if (op == Op::kDelete)
         k_sparse<LOGS, true, false, Loc><<<sg, 128, 0, st>>>(loc, p, parity, sparse_max, status);
@@ -711,15 +763,18 @@ cudaError_t run_phases(const Loc& loc, const Partition& p, Op op, uint32_t spars
         k_sparse<LOGS, false, false, Loc><<<sg, 128, 0, st>>>(loc, p, parity, sparse_max, status);
       count_launch();
     }
-    if (op == Op::kDelete)
-      k_rebuild<LOGS, true, false, Loc><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, sparse_max,
+    // a persistent grid: as many CTAs as fit at once, or as regions exist
+    if (op == Op::kDelete) {
+      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, true, false, Loc>()) : grid;
+      k_rebuild<LOGS, true, false, Loc><<<pg, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, use_list, status);
+    } else if (cnt) {
+      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, false, true, Loc>()) : grid;
+      k_rebuild<LOGS, false, true, Loc><<<pg, 256, Lay<LOGS, true>::BYTES, st>>>(loc, p, parity, use_list, status);
+    } else {
+      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, false, false, Loc>()) : grid;
+      k_rebuild<LOGS, false, false, Loc><<<pg, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, use_list,
                                                                                    status);
-    else if (cnt)
-      k_rebuild<LOGS, false, true, Loc><<<grid, 256, Lay<LOGS, true>::BYTES, st>>>(loc, p, parity, sparse_max,
-                                                                                  status);
-    else
-      k_rebuild<LOGS, false, false, Loc><<<grid, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, sparse_max,
-                                                                                    status);
+    }
     count_launch();
   }
   return cudaGetLastError();
