@@ -9,8 +9,9 @@
 //              requests of one coalescing class (serve_sched.h) into one
 //              launch, admits the group when its bytes fit the free part of
 //              the ring (admission by free device memory), copies the keys
-//              in on a copy stream and enqueues the bulk call and the result
-//              copies on the compute stream;
+//              in on a copy stream, enqueues the bulk call on the compute
+//              stream and a get's result copies on a third stream, so that
+//              they overlap the next launch;
 //   completer  waits for each group's completion event in order, stamps the
 //              requests' latencies, releases their ring space and wakes
 //              waiting clients and the scheduler.
@@ -76,7 +77,7 @@ struct gqf_server {
   uint8_t* staging = nullptr;
   uint64_t staging_bytes = 0;
   uint64_t max_group_keys = 1ULL << 25;
-  cudaStream_t copy = nullptr, comp = nullptr;
+  cudaStream_t copy = nullptr, comp = nullptr, out = nullptr;
   int device = 0;
 
   std::mutex mu;
@@ -113,7 +114,7 @@ cudaEvent_t take_event(gqf_server* s) {
 }
 
 // Enqueues one admitted group; returns false on a launch error.
-bool launch_group(gqf_server* s, Group& g, cudaEvent_t copied) {
+bool launch_group(gqf_server* s, Group& g, cudaEvent_t copied, cudaEvent_t computed) {
   const int op = g.reqs[0].op;
   const int key_is_hash = g.reqs[0].key_is_hash;
   bool reduce = false;
@@ -137,14 +138,18 @@ bool launch_group(gqf_server* s, Group& g, cudaEvent_t copied) {
   int rc = 0;
   if (op == kGet) {
     rc = gqf_bulk_get_async(s->qf, total, keys, outs, flags, s->comp);
+    if (cudaEventRecord(computed, s->comp) != cudaSuccess || cudaStreamWaitEvent(s->out, computed, 0) != cudaSuccess)
+      return false;
     at = 0;
     for (const Request& r : g.reqs) {
       if (rc == 0 && cudaMemcpyAsync(r.counts, outs + at, r.n * 8,
                                      r.on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                     s->comp) != cudaSuccess)
+                                     s->out) != cudaSuccess)
         rc = -1;
       at += r.n;
     }
+    if (cudaEventRecord(g.done, s->out) != cudaSuccess) return false;
+    return rc == 0;
   } else if (op == kDelete) {
     rc = gqf_bulk_delete_async(s->qf, total, keys, flags, s->comp);
   } else if (reduce) {
@@ -158,11 +163,11 @@ bool launch_group(gqf_server* s, Group& g, cudaEvent_t copied) {
 
 void scheduler_main(gqf_server* s) {
   cudaSetDevice(s->device);
-  std::vector<cudaEvent_t> copied_events;
+  std::vector<cudaEvent_t> copied_events, computed_events;
   size_t ce = 0;
   for (;;) {
     Group g;
-    cudaEvent_t copied;
+    cudaEvent_t copied, computed;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
@@ -191,13 +196,17 @@ void scheduler_main(gqf_server* s) {
       g.done = take_event(s);
       s->launching++;
       if (copied_events.size() < 64) {
-        cudaEvent_t e = nullptr;
+        cudaEvent_t e = nullptr, f = nullptr;
         cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&f, cudaEventDisableTiming);
         copied_events.push_back(e);
+        computed_events.push_back(f);
       }
-      copied = copied_events[ce++ % copied_events.size()];
+      copied = copied_events[ce % copied_events.size()];
+      computed = computed_events[ce % computed_events.size()];
+      ce++;
     }
-    g.failed = !launch_group(s, g, copied);
+    g.failed = !launch_group(s, g, copied, computed);
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (g.failed && s->error.empty()) s->error = gqf_last_error();
@@ -209,6 +218,7 @@ void scheduler_main(gqf_server* s) {
   }
   // a stream wait captured each record when it was enqueued: safe to destroy
   for (cudaEvent_t e : copied_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : computed_events) cudaEventDestroy(e);
 }
 
 void finish_request(gqf_server* s, const Request& r, bool failed, Clock::time_point now) {
@@ -277,7 +287,8 @@ int gqf_server_create(QF* qf, uint64_t staging_bytes, gqf_server** out) {
   staging_bytes &= ~255ULL;
   if (staging_bytes < (1ULL << 20) || cudaMalloc((void**)&s->staging, staging_bytes) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&s->comp, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&s->comp, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->out, cudaStreamNonBlocking) != cudaSuccess) {
     if (s->staging) cudaFree(s->staging);
     delete s;
     return -1;
@@ -375,9 +386,11 @@ void gqf_server_destroy(gqf_server* s) {
   s->completer.join();  // completes what is in flight
   cudaStreamSynchronize(s->comp);
   cudaStreamSynchronize(s->copy);
+  cudaStreamSynchronize(s->out);
   for (cudaEvent_t e : s->spare_events) cudaEventDestroy(e);
   cudaStreamDestroy(s->copy);
   cudaStreamDestroy(s->comp);
+  cudaStreamDestroy(s->out);
   cudaFree(s->staging);
   delete s;
 }
