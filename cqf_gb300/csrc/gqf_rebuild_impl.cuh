@@ -66,8 +66,7 @@ struct Lay {
   static constexpr int OFF_RPOS = OFF_KC + KCW * 4;              // u16[WIN + 8] old run ends by rank
   static constexpr int OFF_PREF = OFF_RPOS + (WIN + 8) * 2;      // u16[WIN] lengths, then ends + 1
   static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8] old start, then shift
-  static constexpr int OFF_USED = OFF_DELTA + (WIN + 8) * 2;     // u32[WIN / 32] old run slots
-  static constexpr int OFF_NOCC = (OFF_USED + WIN / 8 + 7) & ~7; // u64[WB] new occupieds
+  static constexpr int OFF_NOCC = (OFF_DELTA + (WIN + 8) * 2 + 7) & ~7;  // u64[WB] new occupieds
   static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
   static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
   static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;     // u16[WB + 8]
@@ -246,7 +245,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
   uint16_t* rpos = reinterpret_cast<uint16_t*>(sm + L::OFF_RPOS);
   uint16_t* pref = reinterpret_cast<uint16_t*>(sm + L::OFF_PREF);
   int16_t* delta = reinterpret_cast<int16_t*>(sm + L::OFF_DELTA);
-  uint32_t* used = reinterpret_cast<uint32_t*>(sm + L::OFF_USED);
   unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
   unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
   uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
@@ -287,7 +285,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     // ---- group this round's keys by quotient (counting sort in shared memory)
     for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
     for (int i = tid; i < WB; i += NT) { nocc[i] = 0; tch[i] = 0; }
-    for (int i = tid; i < WIN / 32; i += NT) used[i] = 0;
     __syncthreads();
     for (int i = tid; i < nk; i += NT) {
       uint32_t q = p.keys[kr + i] >> 8;
@@ -412,8 +409,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
       int ne = runpos(k);  // end of the next old run
       unsigned long long ow = 0, tw = 0;
       int cw = -1;
-      uint32_t ubits = 0;  // used-slot bits of 32-bit word uw
-      int uw = -1;
       for (int q = ca; q < qb_; q++) {
         if ((q >> 6) != cw) {
           cw = q >> 6;
@@ -427,15 +422,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
           const int s = max(q, pe + 1);
           len = e - s + 1;
           delta[k] = (int16_t)s;
-          const int last = min(e, wslots - 1);
-          for (int x = s; x <= last; x++) {  // mark the run's slots
-            if ((x >> 5) != uw) {
-              if (ubits) atomicOr(&used[uw], ubits);
-              uw = x >> 5;
-              ubits = 0;
-            }
-            ubits |= 1u << (x & 31);
-          }
           pe = e;
           k++;
         }
@@ -443,7 +429,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
         pref[q] = (uint16_t)len;
         if (len > 0) { fa = max(q + len - 1, fa + len); fb += len; }
       }
-      if (ubits) atomicOr(&used[uw], ubits);
     }
 
     // ---- run positions: one block-wide max-plus scan over the quotients
@@ -523,19 +508,26 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
       const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
       merge_run<DEL, true>(C, occ, s, e, kg, kn, ks, ke, N, ns);
     }
-    // ---- slot pass: this thread's slots move by their run's shift
+    // ---- slot pass: this thread's slots move by their run's shift.  A slot
+    // after c0 holds part of a run of this window exactly when more of the
+    // window's occupied quotients lie at or before it than runs end before it
+    // (runs never pass a gap), so `o - k` tracks it from the rank tables.
     {
       const int cb = min(ca + QPT, wslots);
       if (ca < cb) {
         int w = ca >> 6;
         unsigned long long m = runs_after_c0(C, w);
+        unsigned long long ow = w < wq_words ? C.occ(w) : 0ULL;
         int k = rrank[w] + __popcll(m & ((1ULL << (ca & 63)) - 1ULL));
+        int o = ca < win_q ? rank_of(ca) : nold;  // occupied window quotients below sl
         for (int sl = ca; sl < cb; sl++) {
           if ((sl >> 6) != w) {
             w = sl >> 6;
             m = runs_after_c0(C, w);
+            ow = w < wq_words ? C.occ(w) : 0ULL;
           }
-          if ((used[sl >> 5] >> (sl & 31)) & 1u) {
+          o += (int)((ow >> (sl & 63)) & 1ULL);
+          if (sl > c0 && o > k) {
             const int d = delta[k];
             if (d != kTouched) {
               const int t = sl + d;
