@@ -453,6 +453,8 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
       int occ_word = ca >> 6, cw = -1;
       unsigned long long ebits = 0;  // new runend bits of window word ew
       int ew = -1;
+      int nlen = ca < qb_ ? pref[ca] : 0;  // the next quotient's length, loaded a step ahead
+      int nd = delta[k];                   // the next run's old start, loaded ahead
       for (int q = ca; q < qb_; q++) {
         if ((q >> 6) != cw) {
           if (cw >= 0 && occ_bits) atomicOr(&nocc[occ_word], occ_bits);
@@ -461,7 +463,8 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
           ow = C.occ(cw);
           tw = q < nq ? tch[cw] : 0ULL;
         }
-        const int len = pref[q];
+        const int len = nlen;
+        if (q + 1 < qb_) nlen = pref[q + 1];
         const int ns = max(q, x + 1);
         if (len > 0) {
           x = ns + len - 1;
@@ -476,8 +479,9 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
           }
         }
         if ((ow >> (q & 63)) & 1ULL) {
-          delta[k] = ((tw >> (q & 63)) & 1ULL) ? kTouched : (int16_t)(ns - delta[k]);
+          delta[k] = ((tw >> (q & 63)) & 1ULL) ? kTouched : (int16_t)(ns - nd);
           k++;
+          nd = delta[k];
         }
         pref[q] = (uint16_t)(x + 1);
       }
