@@ -235,7 +235,7 @@ int do_bulk_reduce(HostFilter* f, uint64_t n, const uint64_t* keys, uint8_t flag
                                        status_ptr(f), st), "merge_tiles") ||
         !ck(launch_partition_counted(f->g, p, f->merge_h, f->merge_c, n, merged_ptr(f), 1, status_ptr(f), st),
             "partition") ||
-        !ck(launch_merge_regions(p, st), "merge_regions"))
+        !ck(launch_merge_regions(p, st, merged_ptr(f), n), "merge_regions"))
       return -1;
   }
   {

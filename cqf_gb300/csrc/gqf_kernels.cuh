@@ -125,12 +125,14 @@ cudaError_t launch_partition_counted(const Geom& g, const Partition& p, const ui
 // Duplicate merging for bulk_insert_reduce.  Tile pass: each CTA merges the
 // equal hashes of a tile of keys in a shared-memory table and appends
 // (hash, count) pairs at out_*[*n_out].  Region pass: regions left with more
-// pairs than one rebuild round takes are merged again in place, shrinking
-// p.region_count.
+// pairs than one rebuild round takes (with n_merged, the pair count of a tile
+// pass over n_in keys, fewer when that pass found heavy duplication) are
+// merged again in place, shrinking p.region_count.
 cudaError_t launch_merge_tiles(const Geom& g, const uint64_t* keys, uint64_t n, int key_is_hash,
                                uint64_t* out_hashes, uint32_t* out_counts, unsigned long long* n_out,
                                uint32_t* status, cudaStream_t st);
-cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st);
+cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st, const unsigned long long* n_merged = nullptr,
+                                 uint64_t n_in = 0);
 
 // K-mers of fixed-length reads (read_len bytes each, ACGT in either case):
 // the tile pass over the canonical k-mers (2-bit packed, first base in the

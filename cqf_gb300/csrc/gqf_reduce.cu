@@ -34,6 +34,7 @@ constexpr int kRegionThreads = 512;
 constexpr int kRegionSlots = 8192;
 constexpr int kRegionMaxDistinct = kRegionSlots / 2;
 constexpr int kRegionSmem = kRegionSlots * (4 + 4);
+constexpr uint32_t kSkewLimit = 64;
 
 __device__ __forceinline__ uint32_t table_slot(uint64_t h, int log_slots) {
   return (uint32_t)((h * 0x9E3779B97F4A7C15ULL) >> (64 - log_slots));  // Fibonacci hashing
@@ -247,7 +248,13 @@ __global__ void __launch_bounds__(256) k_kmers(const uint8_t* __restrict__ reads
 // Merges, in place, the pairs of every region holding more than `limit`
 // (one rebuild round).  A region with more than kRegionMaxDistinct distinct
 // hashes is left as it is: the rebuild then takes it in several rounds.
-__global__ void __launch_bounds__(kRegionThreads) k_merge_regions(Partition p, uint32_t limit) {
+__global__ void __launch_bounds__(kRegionThreads) k_merge_regions(Partition p, uint32_t limit,
+                                                                  const unsigned long long* n_merged,
+                                                                  uint64_t n_in) {
+  // A tile pass that shrank the batch at least fourfold saw heavy
+  // duplication: then every region past kSkewLimit pairs is merged again,
+  // which spares the rebuild most of the repeats arriving from many tiles.
+  if (n_merged && *n_merged * 4 <= n_in) limit = kSkewLimit;
   extern __shared__ __align__(16) uint8_t smem[];
   uint32_t* tk = reinterpret_cast<uint32_t*>(smem);  // local hash + 1, 0 = empty
   uint32_t* tc = reinterpret_cast<uint32_t*>(smem + kRegionSlots * 4);
@@ -388,7 +395,8 @@ cudaError_t launch_kmers(const uint8_t* reads, uint64_t nreads, uint32_t read_le
   return cudaGetLastError();
 }
 
-cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st) {
+cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st, const unsigned long long* n_merged,
+                                 uint64_t n_in) {
   static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(k_merge_regions, cudaFuncAttributeMaxDynamicSharedMemorySize, kRegionSmem);
@@ -398,7 +406,7 @@ cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st) {
   const uint32_t limit = p.log_region >= 13 ? 4096u : 2048u;  // keys one rebuild round takes
   const uint32_t cap = (uint32_t)sm_count() * 3;
   const uint32_t grid = p.nregions < cap ? p.nregions : cap;
-  k_merge_regions<<<grid ? grid : 1, kRegionThreads, kRegionSmem, st>>>(p, limit);
+  k_merge_regions<<<grid ? grid : 1, kRegionThreads, kRegionSmem, st>>>(p, limit, n_merged, n_in);
   count_launch();
   return cudaGetLastError();
 }
