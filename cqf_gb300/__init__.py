@@ -87,6 +87,8 @@ SIGNATURES = {
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
+    "gqf_set_lock_wait": (_int, [_vp, _u32]),
+    "gqf_debug_hold_lock": (_int, [_vp, _u64, _int]),
     "gqf_set_sparse_max": (_int, [_vp, _u32]),
     "gqf_get_sparse_max": (ctypes.c_int64, [_vp]),
     "gqf_nslots": (_u64, [_vp]),
@@ -202,6 +204,12 @@ class QF:
     def set_region_log(self, lr: int):
         if self.L.gqf_set_region_log(self.h, int(lr)) != 0:
             raise ValueError(last_error())
+
+    def set_lock_wait(self, max_spins: int):
+        self._ok(self.L.gqf_set_lock_wait(self.h, max_spins))
+
+    def debug_hold_lock(self, index: int, held: bool = True):
+        self._ok(self.L.gqf_debug_hold_lock(self.h, index, int(held)))
 
     def set_sparse_max(self, n: int):
         self._ok(self.L.gqf_set_sparse_max(self.h, n))

@@ -9,6 +9,7 @@
 //     partition scratch is owned by the filter and grown stream-ordered;
 //   * the filter is built on the device (memset), not on the host and copied.
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -577,6 +578,35 @@ int gqf_get_counters(QF* qf, uint64_t* counters, int n) {
     return -1;
   for (int i = 0; i < n && i < 2; i++) counters[i] = c[i];
   return 0;
+}
+
+int gqf_set_lock_wait(QF* qf, uint32_t max_spins) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  if (max_spins == 0) {
+    set_err("gqf_set_lock_wait: at least one attempt");
+    return -1;
+  }
+  std::lock_guard<std::mutex> lk(f->mu);
+  f->h.lock_spin_limit = max_spins;
+  return ck(cudaMemcpy(reinterpret_cast<uint8_t*>(f->dqf) + offsetof(quotient_filter, lock_spin_limit),
+                       &f->h.lock_spin_limit, sizeof(uint32_t), cudaMemcpyHostToDevice),
+            "cudaMemcpy")
+             ? 0
+             : -1;
+}
+
+int gqf_debug_hold_lock(QF* qf, uint64_t lock_index, int held) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  if (lock_index >= f->h.nlocks) {
+    set_err("gqf_debug_hold_lock: no such lock");
+    return -1;
+  }
+  const uint32_t v = held ? 1u : 0u;
+  return ck(cudaMemcpy(f->h.locks + lock_index * kLockStride, &v, sizeof v, cudaMemcpyHostToDevice), "cudaMemcpy")
+             ? 0
+             : -1;
 }
 
 int gqf_reset(QF* qf) {

@@ -258,6 +258,15 @@ int gqf_set_get_status(gqf_set* s, uint32_t* status);
 /* The filter's default stream for the reference entry points. */
 int gqf_set_stream(QF* qf, void* stream);
 
+/* Point-API lock waits: a lock is tried at most max_spins times (with
+ * growing sleeps, up to about a microsecond each) before the operation gives
+ * up with QF_TIMEOUT and sets GQF_STATUS_TIMEOUT.  Default 2^20.  The
+ * reference spins without a bound (lock_16, src/gqf.cu:2534). */
+int gqf_set_lock_wait(QF* qf, uint32_t max_spins);
+/* Test hook: marks point-API lock `lock_index` (8192-slot region) held or
+ * free, as a thread that died holding it would leave it. */
+int gqf_debug_hold_lock(QF* qf, uint64_t lock_index, int held);
+
 /* Region size of the bulk rebuild: 2^log_region quotients (11, 12 or 13).
  * Does not change results, only speed; 0 restores the automatic choice. */
 int gqf_set_region_log(QF* qf, int log_region);
