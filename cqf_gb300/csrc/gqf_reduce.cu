@@ -251,10 +251,11 @@ __global__ void __launch_bounds__(256) k_kmers(const uint8_t* __restrict__ reads
 __global__ void __launch_bounds__(kRegionThreads) k_merge_regions(Partition p, uint32_t limit,
                                                                   const unsigned long long* n_merged,
                                                                   uint64_t n_in) {
-  // A tile pass that shrank the batch at least fourfold saw heavy
-  // duplication: then every region past kSkewLimit pairs is merged again,
-  // which spares the rebuild most of the repeats arriving from many tiles.
-  if (n_merged && *n_merged * 4 <= n_in) limit = kSkewLimit;
+  // A counted insert (n_merged given) merges every region past kSkewLimit
+  // pairs again: repeats of a key that arrive from many tiles (a hot key, or
+  // a k-mer seen once per covering read) then reach the rebuild once.
+  if (n_merged) limit = kSkewLimit;
+  (void)n_in;
   extern __shared__ __align__(16) uint8_t smem[];
   uint32_t* tk = reinterpret_cast<uint32_t*>(smem);  // local hash + 1, 0 = empty
   uint32_t* tc = reinterpret_cast<uint32_t*>(smem + kRegionSlots * 4);
