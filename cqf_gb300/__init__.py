@@ -87,6 +87,8 @@ SIGNATURES = {
     "gqf_set_stream": (_int, [_vp, _vp]),
     "gqf_set_region_log": (_int, [_vp, _int]),
     "gqf_get_region_log": (_int, [_vp]),
+    "gqf_serialize": (_u64, [_vp, ctypes.c_char_p]),
+    "gqf_deserialize": (_u64, [ctypes.POINTER(_vp), ctypes.c_char_p]),
     "gqf_set_lock_wait": (_int, [_vp, _u32]),
     "gqf_debug_hold_lock": (_int, [_vp, _u64, _int]),
     "gqf_set_sparse_max": (_int, [_vp, _u32]),
@@ -204,6 +206,26 @@ class QF:
     def set_region_log(self, lr: int):
         if self.L.gqf_set_region_log(self.h, int(lr)) != 0:
             raise ValueError(last_error())
+
+    def save(self, path: str) -> int:
+        """Writes the filter image to `path` (gqf_serialize)."""
+        n = int(self.L.gqf_serialize(self.h, os.fsencode(path)))
+        if n == 0:
+            raise RuntimeError(last_error())
+        return n
+
+    @classmethod
+    def load_file(cls, path: str) -> "QF":
+        """A new filter read from a gqf_serialize image (gqf_deserialize)."""
+        L = load()
+        h = _vp()
+        if int(L.gqf_deserialize(ctypes.byref(h), os.fsencode(path))) == 0:
+            raise RuntimeError(last_error())
+        q = cls.__new__(cls)
+        q.L = L
+        q.h = h.value
+        q.nbits = int(L.gqf_nslots(q.h)).bit_length() - 1
+        return q
 
     def set_lock_wait(self, max_spins: int):
         self._ok(self.L.gqf_set_lock_wait(self.h, max_spins))

@@ -692,6 +692,58 @@ int gqf_import(QF* qf, const void* host_buf, uint64_t len) {
   return 0;
 }
 
+uint64_t gqf_serialize(QF* qf, const char* path) {
+  HostFilter* f = lookup(qf);
+  if (!f || !path) return 0;
+  std::vector<uint8_t> img(120 + f->h.nblocks * 81);
+  if (gqf_export(qf, img.data(), img.size()) != 0) return 0;
+  FILE* fh = std::fopen(path, "wb");
+  if (!fh) {
+    set_err(std::string("gqf_serialize: cannot open ") + path);
+    return 0;
+  }
+  const size_t w = std::fwrite(img.data(), 1, img.size(), fh);
+  const bool good = std::fclose(fh) == 0 && w == img.size();
+  if (!good) set_err(std::string("gqf_serialize: short write to ") + path);
+  return good ? (uint64_t)w : 0;
+}
+
+uint64_t gqf_deserialize(QF** out, const char* path) {
+  if (!out || !path) return 0;
+  *out = nullptr;
+  FILE* fh = std::fopen(path, "rb");
+  if (!fh) {
+    set_err(std::string("gqf_deserialize: cannot open ") + path);
+    return 0;
+  }
+  uint64_t meta[15] = {0};
+  if (std::fread(meta, 1, 120, fh) != 120 || meta[0] != 1018874902021329732ULL || meta[9] != 8 ||
+      meta[4] == 0 || (meta[4] & (meta[4] - 1)) != 0) {
+    std::fclose(fh);
+    set_err("gqf_deserialize: not a filter image with 8-bit slots");
+    return 0;
+  }
+  int nbits = 0;
+  while ((1ULL << nbits) < meta[4]) nbits++;
+  std::vector<uint8_t> img(120 + 81 * meta[11]);
+  std::memcpy(img.data(), meta, 120);
+  const size_t r = std::fread(img.data() + 120, 1, img.size() - 120, fh);
+  std::fclose(fh);
+  if (r != img.size() - 120) {
+    set_err("gqf_deserialize: truncated image");
+    return 0;
+  }
+  QF* q = nullptr;
+  qf_malloc_device(&q, nbits, true);
+  if (!q) return 0;
+  if (gqf_import(q, img.data(), img.size()) != 0) {
+    qf_destroy_device(q);
+    return 0;
+  }
+  *out = q;
+  return img.size();
+}
+
 int gqf_profile(QF* qf, int enable) {
   HostFilter* f = lookup(qf);
   if (!f) return -1;

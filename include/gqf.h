@@ -258,6 +258,14 @@ int gqf_set_get_status(gqf_set* s, uint32_t* status);
 /* The filter's default stream for the reference entry points. */
 int gqf_set_stream(QF* qf, void* stream);
 
+/* Files (the reference declares qf_serialize / qf_deserialize,
+ * include/gqf_file.cuh:46-49, for host filters): the gqf_export image (the
+ * reference's 120-byte metadata and packed 81-byte blocks) written to or read
+ * from `path`.  gqf_deserialize allocates a filter of the image's size into
+ * *qf.  Both return the bytes written / read, 0 on error. */
+uint64_t gqf_serialize(QF* qf, const char* path);
+uint64_t gqf_deserialize(QF** qf, const char* path);
+
 /* Point-API lock waits: a lock is tried at most max_spins times (with
  * growing sleeps, up to about a microsecond each) before the operation gives
  * up with QF_TIMEOUT and sets GQF_STATUS_TIMEOUT.  Default 2^20.  The

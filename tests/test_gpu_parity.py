@@ -392,3 +392,28 @@ def test_batched_fill_matches_oracle(gq, nbits):
         qf.bulk_delete(dev(keys[: n // 4]))
         a, b = o.dump(), qf.export()
         assert np.array_equal(a, b), first_diff(a, b)
+
+
+def test_serialize_roundtrip_and_reference_image(gq, golden, tmp_path):
+    """gqf_serialize / gqf_deserialize: a file round trip keeps the filter,
+    and an image of the reference's own filter (the golden dump) loads."""
+    meta, arrays = golden
+    nbits = 14
+    keys = oracle.splitmix64(1, meta["uniform14"]["n"])
+    path = str(tmp_path / "f.gqf")
+    with gq.QF(nbits) as qf:
+        qf.bulk_insert(dev(keys))
+        n = qf.save(path)
+        assert n == 120 + 81 * qf.nblocks
+        with gq.QF.load_file(path) as back:
+            assert back.nbits == nbits
+            assert np.array_equal(back.export(), qf.export())
+            assert np.array_equal(gpu_get(back, keys), gpu_get(qf, keys))
+    ref = arrays["uniform14_dump_insert"] if "uniform14_dump_insert" in arrays else None
+    if ref is not None:
+        (tmp_path / "ref.gqf").write_bytes(np.ascontiguousarray(ref).tobytes())
+        with gq.QF.load_file(str(tmp_path / "ref.gqf")) as r:
+            assert np.array_equal(r.export(), ref)
+    (tmp_path / "bad.gqf").write_bytes(b"not a filter")
+    with pytest.raises(RuntimeError):
+        gq.QF.load_file(str(tmp_path / "bad.gqf"))
