@@ -200,6 +200,26 @@ def profile_traffic():
     return out
 
 
+# ------------------------------------------------------ replicas (N > 1)
+
+def max_over_ranks(x: float, dist=None, device="cuda") -> float:
+    """The slowest rank's time (or any per-rank figure's maximum); x itself
+    when running alone.  Works with NCCL (device tensors) and gloo (CPU)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job Mkeys/s: every rank processed units_per_rank in at most
+    `seconds` (the slowest rank's time)."""
+    return units_per_rank * world / seconds / 1e6
+
+
 # --------------------------------------------------------------- GPU arm
 
 def run_gpu(args, wl, rank, world):
@@ -281,12 +301,8 @@ def run_gpu(args, wl, rank, world):
     qf.profile(False)
     clk = clocks.stop()
     status = qf.status()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-
-    value = wl.key_ops * world / (ms * 1e-3) / 1e6
+    ms = max_over_ranks(ms, dist)
+    value = job_rate(wl.key_ops, world, ms * 1e-3)
     ops = {k: {"ms": v / args.steps} for k, v in per.items()}
     ops["insert"]["mkeys_s"] = wl.n_insert / (ops["insert"]["ms"] * 1e3)
     ops["get"]["mkeys_s"] = 2 * wl.n_get / (ops["get"]["ms"] * 1e3)
@@ -343,7 +359,7 @@ def run_gpu(args, wl, rank, world):
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, wl, qf, keys, absent, torch)
+        e2e = run_e2e(args, wl, qf, keys, absent, torch, dist, world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -403,7 +419,7 @@ def run_gpu(args, wl, rank, world):
     return line
 
 
-def run_e2e(args, wl, qf, keys_dev, absent_dev, torch):
+def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
     """The same step through the C ABI from pinned host buffers: every batch
     is copied host->device inside the timed region, get results come back
     device->host.  Copies overlap compute on a second stream."""
@@ -461,12 +477,12 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch):
     for _ in range(args.steps):
         step()
     torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / args.steps
+    dt = max_over_ranks((time.perf_counter() - t0) / args.steps, dist)
     qf.set_stream(None)
     found = bool((hres[: wl.n_get] > 0).all().item())
     h2d = 8 * (wl.n_insert + 2 * wl.n_get + wl.n_get)
     return {
-        "value": round(wl.key_ops / dt / 1e6, 2),
+        "value": round(job_rate(wl.key_ops, world, dt), 2),
         "unit": UNIT,
         "ms_per_step": round(dt * 1e3, 3),
         "h2d_bytes_per_step": h2d,
