@@ -1,9 +1,9 @@
-"""The reference's own CUDA build, driven on a GPU -- TEST/BENCH INFRASTRUCTURE.
+"""The reference's own CUDA build, driven on a GPU -- BENCH/TEST INFRASTRUCTURE.
 
-oracle/ref/Makefile compiles the reference's device code (src/gqf.cu +
-src/hashutil.cu, unmodified) into oracle/_ref/gqf_ref_sm103a.cubin on the x86
+baseline.build() compiles the reference's device code (src/gqf.cu +
+src/hashutil.cu, unmodified) into baseline/_ref/gqf_ref_sm103a.cubin on the
 host that has the reference tree, and records the byte layout of its structs
-(oracle/_ref/refgpu_layout.json).  The reference's host code is x86-only, so
+(baseline/_ref/refgpu_layout.json).  The reference's host code is x86-only, so
 this module restates its host orchestration and launches its kernels through
 the CUDA driver API:
 
@@ -33,7 +33,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CUBIN = os.path.join(HERE, "_ref", "gqf_ref_sm103a.cubin")
+CUBIN = os.path.join(HERE, "_ref", "gqf_ref_sm103a.cubin")  # baseline/_ref
 LAYOUT = os.path.join(HERE, "_ref", "refgpu_layout.json")
 
 KERNELS = {

@@ -494,11 +494,11 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
 
 def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
     """The reference's own CUDA build (its kernels compiled from its sources,
-    driven by oracle/refgpu.py) on the same step, timed per call by wall
+    driven by baseline/refgpu.py) on the same step, timed per call by wall
     clock around a synchronised call (the reference synchronises inside each
     bulk call).  Keys are copied to a scratch buffer before each call, outside
     the timing, because the reference overwrites them."""
-    from oracle import refgpu
+    from baseline import refgpu
 
     if not refgpu.available():
         return {"unavailable": "reference cubin not built (needs the reference tree on an x86 host)"}
@@ -550,7 +550,7 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
         },
         "present_all_found": found,
         "what": "reference src/gqf.cu kernels compiled for sm_103a from its sources; host orchestration "
-                "restated (oracle/refgpu.py), thrust::sort replaced by torch.sort",
+                "restated (baseline/refgpu.py), thrust::sort replaced by torch.sort",
     }
 
 
@@ -583,7 +583,7 @@ def run_skew(args, torch, cqf_gb300):
     bulk_insert_reduce; (ii) canonical 31-mers of 2^20 150-bp reads (seed 4,
     1% substitutions, genome of 2^24 bases) through gqf_bulk_insert_kmers.
     Timed end to end on the device (events) per call, after warm-up; the
-    reference's CUDA reduce path (oracle/refgpu.py) on the same multisets."""
+    reference's CUDA reduce path (baseline/refgpu.py) on the same multisets."""
     from cqf_gb300 import synth
 
     nbits = 28
@@ -614,7 +614,7 @@ def run_skew(args, torch, cqf_gb300):
                          "ms": round(tmed * 1e3, 3), "keys": n, "units": units, "distinct": distinct,
                          "exact_counts_equal": ok, "status": qf.status()}
     if not args.no_ref_cuda:
-        from oracle import refgpu
+        from baseline import refgpu
 
         if refgpu.available():
             scratch = torch.empty(keys.numel(), dtype=torch.int64, device="cuda")
@@ -717,7 +717,7 @@ def run_batched(args, torch, cqf_gb300):
         "present_all_found": found, "false_positives": fp, "status": status,
     }
     if not args.no_ref_cuda:
-        from oracle import refgpu
+        from baseline import refgpu
 
         if refgpu.available():
             out = torch.empty(int(sizes.max()), dtype=torch.int64, device="cuda")
@@ -744,7 +744,7 @@ def run_batched(args, torch, cqf_gb300):
                                "seconds_all_filters_est": round(ops / rate / 1e6, 1),
                                "present_found_sampled": ok,
                                "what": "per filter: device buffers + bulk_insert + bulk_get x2 of the reference's "
-                                       "kernels (oracle/refgpu.py), synchronised as its API is; every 16th "
+                                       "kernels (baseline/refgpu.py), synchronised as its API is; every 16th "
                                        "filter timed, rate over the sample's key operations"}
             res["speedup_vs_ref_cuda"] = round((ops / ms / 1e3) / rate, 1)
     del keys, absent, cp, ca
@@ -923,7 +923,7 @@ def run_serving(args, torch, cqf_gb300):
 
 
 def run_serving_ref(st, nbits, pool, rate, torch):
-    from oracle import refgpu
+    from baseline import refgpu
 
     if not refgpu.available():
         return {"unavailable": "reference cubin not built"}

@@ -48,25 +48,7 @@ def build_ref() -> str | None:
     if platform.machine() not in ("x86_64", "AMD64") or not os.path.isdir(REFERENCE_TREE):
         return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={REFERENCE_TREE}"])
-    write_ref_layout()
     return REF_LIB_PATH
-
-
-def write_ref_layout() -> str:
-    """Record the reference's struct layout (as its compiler laid it out) for
-    oracle/refgpu.py, which builds those structs in device memory."""
-    import json
-
-    L = ctypes.CDLL(REF_LIB_PATH)
-    a = (ctypes.c_uint64 * 12)()
-    L.ref_layout(a)
-    names = ["sizeof_QF", "QF_runtimedata", "QF_metadata", "QF_blocks", "sizeof_qfruntime",
-             "qfruntime_num_locks", "qfruntime_locks", "qfruntime_buffers", "qfruntime_buffer_sizes",
-             "sizeof_qfmetadata", "sizeof_qfblock", "qfruntime_wait_times"]
-    path = os.path.join(REF_DIR, "refgpu_layout.json")
-    with open(path, "w") as fh:
-        json.dump({k: int(v) for k, v in zip(names, a)}, fh, indent=1)
-    return path
 
 
 def splitmix64(seed: int, n: int) -> np.ndarray:

@@ -1,5 +1,5 @@
 """The reference's own CUDA build (its kernels compiled from its sources,
-oracle/refgpu.py) agrees with the oracle and with the product on small
+baseline/refgpu.py) agrees with the oracle and with the product on small
 filters.  Skipped where the cubin was not built (it needs the reference
 tree on an x86 host)."""
 import numpy as np
@@ -17,7 +17,7 @@ def refgpu():
 
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    from oracle import refgpu
+    from baseline import refgpu
 
     if not refgpu.available():
         pytest.skip("reference cubin not built here")
