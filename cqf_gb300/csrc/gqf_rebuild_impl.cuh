@@ -40,9 +40,9 @@ struct Cfg;
 template <>
 struct Cfg<11> { static constexpr int PUSH = 1024, KMAX = 2048, MINB = 4; };
 template <>
-struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 3; };
+struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 4; };
 template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 1; };
+struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 2; };
 
 template <int LOGS, bool CNT>
 struct Lay {
@@ -55,17 +55,22 @@ struct Lay {
   static constexpr int QPT = WIN / NT;
   static constexpr int KCW = REG / 2 + 2;  // packed 16-bit per-quotient key counters
   static_assert(WIN % NT == 0 && (REG / 2) % NT == 0, "work splits evenly over threads");
+  static_assert(KCW * 4 <= (WIN + 8) * 2, "the key counters fit the shift table they share");
   static_assert(PUSH < REG, "a window must not reach the region after next");
   static_assert(WIN + PUSH + 64 < 32767, "window positions fit int16");
+  static_assert(WB < NT, "window words fit one scan");
+  static_assert(WIN + PUSH < 16384, "shifts and old starts fit apart in int16");
   // shared memory carve-up (bytes)
   static constexpr int IMG = WB * 96;
   static constexpr int OFF_IMG0 = 0;
   static constexpr int OFF_IMG1 = OFF_IMG0 + IMG;
   static constexpr int OFF_KG = OFF_IMG1 + IMG;                  // u32[KMAX] keys grouped by quotient
-  static constexpr int OFF_KC = OFF_KG + KMAX * 4;               // u32[KCW]
-  static constexpr int OFF_RPOS = OFF_KC + KCW * 4;              // u16[WIN + 8] old run ends by rank
-  static constexpr int OFF_PREF = OFF_RPOS + (WIN + 8) * 2;      // u16[WIN] lengths, then ends + 1
-  static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8] old start, then shift
+  static constexpr int OFF_PREF = OFF_KG + KMAX * 4;             // u16[WIN] lengths, then ends + 1
+  // one table, three lives: the key counters while the keys are grouped,
+  // then the old run ends by rank, then each old run's start and shift
+  static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8]
+  static constexpr int OFF_KC = OFF_DELTA;                       // u32[KCW]
+  static constexpr int OFF_RPOS = OFF_DELTA;                     // u16[WIN + 8]
   static constexpr int OFF_NOCC = (OFF_DELTA + (WIN + 8) * 2 + 7) & ~7;  // u64[WB] new occupieds
   static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
   static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
@@ -74,7 +79,9 @@ struct Lay {
   static constexpr int BYTES = OFF_KN + (CNT ? KMAX * 4 : 0);
 };
 
-constexpr int16_t kTouched = 0x7FFF;  // shift marker: the run is rewritten by its merge
+// A run rewritten by its merge keeps kTouched + its old start in the shift
+// table; untouched runs hold their shift, always below kTouched.
+constexpr int kTouched = 16384;
 // The work list of one phase lives in the partition's cursor array (free once
 // the keys are scattered): [0] regions listed by k_sparse, [1] the next one
 // a rebuild CTA takes, [2 ...] the region indices.
@@ -242,13 +249,13 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
 
   uint32_t* kg = reinterpret_cast<uint32_t*>(sm + L::OFF_KG);
   uint32_t* kc = reinterpret_cast<uint32_t*>(sm + L::OFF_KC);
-  uint16_t* rpos = reinterpret_cast<uint16_t*>(sm + L::OFF_RPOS);
   uint16_t* pref = reinterpret_cast<uint16_t*>(sm + L::OFF_PREF);
   int16_t* delta = reinterpret_cast<int16_t*>(sm + L::OFF_DELTA);
   unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
   unsigned long long* tch = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);
   uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
   uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
+  uint16_t* rpos = reinterpret_cast<uint16_t*>(sm + L::OFF_RPOS);
   uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
 
   // ---- stage the window (wb blocks of 96 bytes) into image 0
@@ -267,7 +274,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
   int cur = 0;
   bool changed = false;
 
-  auto kcnt = [&](int q) -> int { return (int)((kc[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu); };
   // runends of word w that lie after c0
   auto runs_after_c0 = [&](Img C, int w) -> unsigned long long {
     unsigned long long rw = C.run(w);
@@ -315,7 +321,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
       kg[(old >> sh) & 0xFFFFu] = key;
       if (CNT) kn[(old >> sh) & 0xFFFFu] = p.counts[kr + i];
     }
-    // now the keys of quotient q are kg[q ? kcnt(q-1) : 0, kcnt(q))
+    // now the keys of each quotient are contiguous in kg, in quotient order
 
     // ---- rank tables of the current image: per window word, the occupied
     // quotients and the runends after c0 before it (one packed block scan)
@@ -358,8 +364,15 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     }
     __syncthreads();
 
+    // Runs ending beyond the window get positions past it, in order.
     const int fake0 = win_valid + 16;
     auto runpos = [&](int k) -> int { return k < nvis ? (int)rpos[k] : fake0 + (k - nvis); };
+    // the end of a quotient's key group in kg
+    auto group_end = [&](int ks, uint32_t q) -> int {
+      int ke = ks + 1;
+      while (ke < nk && (kg[ke] >> 8) == q) ke++;
+      return ke;
+    };
     auto rank_of = [&](int q) -> int {
       return (int)orank[q >> 6] + __popcll(C.occ(q >> 6) & ((1ULL << (q & 63)) - 1ULL));
     };
@@ -370,7 +383,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     for (int i = tid; i < nk; i += NT) {
       const uint32_t q = kg[i] >> 8;
       if (i > 0 && (kg[i - 1] >> 8) == q) continue;
-      const int ks = i, ke = kcnt((int)q);
+      const int ks = i, ke = group_end(i, q);
       atomicOr(&tch[q >> 6], 1ULL << (q & 63));
       const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
       int s = 0, e = -1;
@@ -402,11 +415,15 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     // ---- this thread's quotients: old runs, new lengths, composed max-plus map
     const int qb_ = min(ca + QPT, win_q);
     const int k0 = ca < win_q ? rank_of(ca) : nold;
+    const int e_old = nold ? runpos(nold - 1) : c0;  // end of the window's old runs
     int fa = kNeg, fb = 0;
     {
       int k = k0;
       int pe = k ? runpos(k - 1) : c0;
-      int ne = runpos(k);  // end of the next old run
+      // From here the table turns from run ends into run starts, each thread
+      // over its own runs [k0, k1): the run ends other threads read (k0 - 1
+      // above, e_old) are read before any is overwritten.
+      __syncthreads();
       unsigned long long ow = 0, tw = 0;
       int cw = -1;
       for (int q = ca; q < qb_; q++) {
@@ -417,8 +434,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
         }
         int len = 0;
         if ((ow >> (q & 63)) & 1ULL) {
-          const int e = ne;
-          ne = runpos(k + 1);
+          const int e = runpos(k);
           const int s = max(q, pe + 1);
           len = e - s + 1;
           delta[k] = (int16_t)s;
@@ -479,7 +495,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
           }
         }
         if ((ow >> (q & 63)) & 1ULL) {
-          delta[k] = ((tw >> (q & 63)) & 1ULL) ? kTouched : (int16_t)(ns - nd);
+          delta[k] = (int16_t)(((tw >> (q & 63)) & 1ULL) ? kTouched + nd : ns - nd);
           k++;
           nd = delta[k];
         }
@@ -490,7 +506,6 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     }
     __syncthreads();
     {
-      const int e_old = nold ? runpos(nold - 1) : c0;
       const int e_new = (int)pref[win_q - 1] - 1;
       // A change that reaches the window's end would move runs this CTA does
       // not hold (or overflow the table): leave the region to the serial pass.
@@ -501,13 +516,15 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
       const uint32_t q = kg[i] >> 8;
       if (i > 0 && (kg[i - 1] >> 8) == q) continue;
       if (!((nocc[q >> 6] >> (q & 63)) & 1ULL)) continue;  // deleted entirely
-      const int ks = i, ke = kcnt((int)q);
+      const int ks = i, ke = group_end(i, q);
       const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
       int s = 0, e = -1;
-      if (occ) {
-        const int k = rank_of((int)q);
-        e = runpos(k);
-        s = max((int)q, (k ? runpos(k - 1) : c0) + 1);
+      if (occ) {  // the old run: its start kept by the apply, its end the next runend
+        s = (int)delta[rank_of((int)q)] - kTouched;
+        int w = s >> 6;
+        unsigned long long m = C.run(w) & (~0ULL << (s & 63));
+        while (!m) m = C.run(++w);  // ends below win_valid: the first merge deferred the rest
+        e = 64 * w + __ffsll((long long)m) - 1;
       }
       const int ns = max((int)q, (q ? (int)pref[q - 1] - 1 : c0) + 1);
       merge_run<DEL, true>(C, occ, s, e, kg, kn, ks, ke, N, ns);
@@ -533,7 +550,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
           o += (int)((ow >> (sl & 63)) & 1ULL);
           if (sl > c0 && o > k) {
             const int d = delta[k];
-            if (d != kTouched) {
+            if (d < kTouched) {
               const int t = sl + d;
               if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
             }
