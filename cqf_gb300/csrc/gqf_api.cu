@@ -176,13 +176,14 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
     uint32_t cap = nr + 2;
     if (f->part.region_count) cudaFreeAsync(f->part.region_count, st);
     uint32_t* base = nullptr;
-    // region_count | region_start | cursor | deferred, one allocation
-    if (!ck(cudaMallocAsync((void**)&base, 4ULL * cap * sizeof(uint32_t), st), "cudaMallocAsync regions"))
+    // region_count | region_start | cursor | deferred | retry, one allocation
+    if (!ck(cudaMallocAsync((void**)&base, 5ULL * cap * sizeof(uint32_t), st), "cudaMallocAsync regions"))
       return false;
     f->part.region_count = base;
     f->part.region_start = base + cap;
     f->part.cursor = base + 2ULL * cap;
     f->part.deferred = base + 3ULL * cap;
+    f->part.retry = base + 4ULL * cap;
     f->region_cap = cap;
   }
   f->part.nregions = nr;

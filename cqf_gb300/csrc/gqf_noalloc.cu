@@ -65,9 +65,10 @@ extern "C" int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* k
 
   std::lock_guard<std::mutex> lk(*static_cast<std::mutex*>(v.mu));
   internal_view(qf, &v);  // geometry as of now, under the filter's lock
-  // four per-region tables (counts, starts, cursors, deferred list), then keys
+  // five per-region tables (counts, starts, cursors, deferred and retry
+  // lists), then keys
   const uint64_t words = (uint64_t)v.nregions + 2;
-  const uint64_t table_bytes = (16 * words + 255) & ~255ULL;
+  const uint64_t table_bytes = (20 * words + 255) & ~255ULL;
   const uint64_t max_keys = table_bytes < GQF_NOALLOC_SCRATCH_BYTES
                                 ? (GQF_NOALLOC_SCRATCH_BYTES - table_bytes) / sizeof(uint32_t)
                                 : 0;
@@ -92,6 +93,7 @@ extern "C" int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* k
   p.region_start = w + words;
   p.cursor = w + 2 * words;
   p.deferred = w + 3 * words;
+  p.retry = w + 4 * words;
   p.keys = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + table_bytes);
   p.counts = nullptr;
   p.stats = v.stats;

@@ -37,12 +37,14 @@ constexpr int kNeg = -(1 << 28);  // "minus infinity" of the max-plus scan
 
 template <int LOGS>
 struct Cfg;
+// PUSH: the slots past the region a window holds; TAIL: the shorter tail
+// tried first, enough whenever the region's growth is absorbed that close.
 template <>
-struct Cfg<11> { static constexpr int PUSH = 1024, KMAX = 2048, MINB = 4; };
+struct Cfg<11> { static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4; };
 template <>
-struct Cfg<12> { static constexpr int PUSH = 2048, KMAX = 2048, MINB = 4; };
+struct Cfg<12> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 2048, MINB = 4; };
 template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, KMAX = 4096, MINB = 2; };
+struct Cfg<13> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 4096, MINB = 2; };
 
 template <int LOGS, bool CNT>
 struct Lay {
@@ -51,10 +53,11 @@ struct Lay {
   static constexpr int PUSH = Cfg<LOGS>::PUSH;
   static constexpr int KMAX = Cfg<LOGS>::KMAX;
   static constexpr int WIN = REG + PUSH;
+  static constexpr int SHORT = REG + Cfg<LOGS>::TAIL;
   static constexpr int WB = WIN / 64;
-  static constexpr int QPT = WIN / NT;
   static constexpr int KCW = REG / 2 + 2;  // packed 16-bit per-quotient key counters
-  static_assert(WIN % NT == 0 && (REG / 2) % NT == 0, "work splits evenly over threads");
+  static_assert(WIN % NT == 0 && SHORT % NT == 0 && SHORT <= WIN && (REG / 2) % NT == 0,
+                "work splits evenly over threads");
   static_assert(KCW * 4 <= (WIN + 8) * 2, "the key counters fit the shift table they share");
   static_assert(PUSH < REG, "a window must not reach the region after next");
   static_assert(WIN + PUSH + 64 < 32767, "window positions fit int16");
@@ -220,30 +223,33 @@ __device__ int scan_sum(int v, int* tmp, int* total) {
 
 // CNT: the batch carries a multiplicity per key (p.counts), as produced by
 // the duplicate-merging pass of bulk_insert_reduce.
-// Rebuilds region R of the launch (all threads of the CTA).
-template <int LOGS, bool DEL, bool CNT, class Loc>
-__device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& p, const uint32_t R,
-                                               uint32_t* status) {
+// Rebuilds region R of the launch (all threads of the CTA) in a window of
+// SPAN slots (a multiple of the thread count, at most the full window);
+// returns false, having written nothing, when the changes would reach past
+// the window.
+template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
+__device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& p, const uint32_t R) {
   using L = Lay<LOGS, CNT>;
-  constexpr int NT = L::NT, WB = L::WB, WIN = L::WIN, REG = L::REG, KMAX = L::KMAX, QPT = L::QPT;
+  constexpr int NT = L::NT, WB = L::WB, REG = L::REG, KMAX = L::KMAX, span = SPAN;
+  constexpr int qpt = SPAN / NT;  // slots and quotients per thread
   extern __shared__ __align__(128) uint8_t sm[];
   __shared__ int s_i[8];
   __shared__ int sa[32], sb[32];
 
   const uint32_t kbeg = p.region_start[R], kend = kbeg + p.region_count[R];
-  if (kbeg == kend) return;
+  if (kbeg == kend) return true;
   Geom g;
   uint32_t r;  // the region within its filter
   const quotient_filter* dq;
-  if (!loc.locate(R, LOGS, &g, &r, &dq)) return;
+  if (!loc.locate(R, LOGS, &g, &r, &dq)) return true;
   const int tid = threadIdx.x;
 
   const uint64_t base = (uint64_t)r << LOGS;
   const uint64_t bw0 = base >> 6;
-  const int wb = (int)min((uint64_t)WB, g.nblocks - bw0);
+  const int wb = (int)min((uint64_t)(span / 64), g.nblocks - bw0);
   const int wslots = wb * 64;
   const int win_valid = (int)min((uint64_t)wslots, g.xnslots - base);
-  const int win_q = (int)min((uint64_t)WIN, g.nslots - base);
+  const int win_q = (int)min((uint64_t)span, g.nslots - base);
   const int wq_words = (win_q + 63) >> 6;
   const int nq = (int)min((uint64_t)REG, g.nslots - base);
 
@@ -342,11 +348,11 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     }
     __syncthreads();
     const int nvis = s_i[0], nold = s_i[1];
-    // Each thread owns QPT consecutive slots / quotients from here on, so
+    // Each thread owns qpt consecutive slots / quotients from here on, so
     // ranks, run ends and shifts carry from one to the next in registers.
-    const int ca = tid * QPT;
+    const int ca = tid * qpt;
     {  // rpos[k] = the k-th runend after c0, for this thread's slots
-      const int cb = min(ca + QPT, wslots);
+      const int cb = min(ca + qpt, wslots);
       int x = ca;
       while (x < cb) {
         const int w = x >> 6;
@@ -413,7 +419,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     if (__syncthreads_or(my_defer)) { deferred = true; break; }
 
     // ---- this thread's quotients: old runs, new lengths, composed max-plus map
-    const int qb_ = min(ca + QPT, win_q);
+    const int qb_ = min(ca + qpt, win_q);
     const int k0 = ca < win_q ? rank_of(ca) : nold;
     const int e_old = nold ? runpos(nold - 1) : c0;  // end of the window's old runs
     int fa = kNeg, fb = 0;
@@ -534,7 +540,7 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     // window's occupied quotients lie at or before it than runs end before it
     // (runs never pass a gap), so `o - k` tracks it from the rank tables.
     {
-      const int cb = min(ca + QPT, wslots);
+      const int cb = min(ca + qpt, wslots);
       if (ca < cb) {
         int w = ca >> 6;
         unsigned long long m = runs_after_c0(C, w);
@@ -576,16 +582,8 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
     changed = true;
   }
 
-  if (deferred) {
-    if (tid == 0) {
-      uint32_t at = atomicAdd(&p.deferred[0], 1u);
-      p.deferred[1 + at] = R;
-      atomicOr(status, kStDeferred);
-      if (p.stats) atomicAdd(&p.stats[0], 1ULL);
-    }
-    return;
-  }
-  if (!changed) return;
+  if (deferred) return false;
+  if (!changed) return true;
   // ---- write back the blocks that differ from what was loaded
   {
     const uint4* fin = reinterpret_cast<const uint4*>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
@@ -602,29 +600,54 @@ __device__ __forceinline__ void rebuild_region(const Loc& loc, const Partition& 
         for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
     }
   }
+  return true;
 }
 
-// The rebuild of one phase.  With a work list (key-by-key updates on): a
-// persistent grid whose CTAs take the regions k_sparse listed, one at a
-// time, until the list is exhausted.  Without: one CTA per region of the
-// parity, in region order.
-template <int LOGS, bool DEL, bool CNT, class Loc>
+// Where a rebuild launch finds its regions: one CTA per region of the
+// parity, in region order; or a persistent grid whose CTAs take regions
+// one at a time from a work list (k_sparse's, or the short pass's retries)
+// until it is exhausted.
+enum : int { kFromGrid = 0, kFromList = 1, kFromRetry = 2 };
+
+// The rebuild of one phase in windows of SPAN slots.  The short pass
+// (SPAN < the full window) lists for the full pass the regions it cannot
+// hold, and those whose keys need several rounds (they may grow further);
+// the full pass leaves what it cannot hold to the serial fallback.
+template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
-                                                                             int use_list, uint32_t* status) {
-  if (!use_list) {
+                                                                             int from, uint32_t* status) {
+  using L = Lay<LOGS, CNT>;
+  constexpr bool kShort = SPAN < L::WIN;
+  auto one = [&](uint32_t R) {
+    const bool ok = (kShort && p.region_count[R] > (uint32_t)L::KMAX)
+                        ? false
+                        : rebuild_window<LOGS, DEL, CNT, SPAN>(loc, p, R);
+    if (ok || threadIdx.x != 0) return;
+    if (kShort) {
+      const uint32_t at = atomicAdd(&p.retry[kListCount], 1u);
+      p.retry[kListBase + at] = R;
+    } else {
+      const uint32_t at = atomicAdd(&p.deferred[0], 1u);
+      p.deferred[1 + at] = R;
+      atomicOr(status, kStDeferred);
+      if (p.stats) atomicAdd(&p.stats[0], 1ULL);
+    }
+  };
+  if (from == kFromGrid) {
     const uint32_t R = 2 * blockIdx.x + parity;
-    if (R < p.nregions) rebuild_region<LOGS, DEL, CNT>(loc, p, R, status);
+    if (R < p.nregions) one(R);
     return;
   }
+  uint32_t* list = from == kFromList ? p.cursor : p.retry;
   __shared__ uint32_t s_take;
-  const uint32_t count = p.cursor[kListCount];
+  const uint32_t count = list[kListCount];  // complete: the launch that fills it has ended
   for (;;) {
     __syncthreads();  // the previous region is written back before its memory is reused
-    if (threadIdx.x == 0) s_take = atomicAdd(&p.cursor[kListNext], 1u);
+    if (threadIdx.x == 0) s_take = atomicAdd(&list[kListNext], 1u);
     __syncthreads();
     const uint32_t i = s_take;
     if (i >= count) return;
-    rebuild_region<LOGS, DEL, CNT>(loc, p, p.cursor[kListBase + i], status);
+    one(list[kListBase + i]);
   }
 }
 
@@ -727,28 +750,46 @@ __global__ void k_fallback(Loc loc, Partition p, int del, uint32_t* status) {
   }
 }
 
-template <int LOGS, bool DEL, bool CNT, class Loc>
+template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 void configure() {
   static bool done = false;  // per instantiation
   if (done) return;
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, Loc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        Lay<LOGS, CNT>::BYTES);
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, Loc>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   done = true;
 }
 
 // CTAs of k_rebuild resident at once on the device.
-template <int LOGS, bool DEL, bool CNT, class Loc>
+template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 uint32_t resident() {
   static uint32_t n = 0;  // per instantiation
   if (!n) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild<LOGS, DEL, CNT, Loc>, 256, Lay<LOGS, CNT>::BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, 256,
+                                                  Lay<LOGS, CNT>::BYTES);
     n = (uint32_t)std::max(1, sms) * (uint32_t)std::max(1, per);
   }
   return n;
+}
+
+// The two passes of one parity: the short windows over the grid or the
+// listed regions, then the full windows over the short pass's retries.
+template <int LOGS, bool DEL, bool CNT, class Loc>
+void launch_passes(const Loc& loc, const Partition& p, int parity, int use_list, uint32_t grid, uint32_t* status,
+                   cudaStream_t st) {
+  using L = Lay<LOGS, CNT>;
+  configure<LOGS, DEL, CNT, L::SHORT, Loc>();
+  configure<LOGS, DEL, CNT, L::WIN, Loc>();
+  const uint32_t g1 = use_list ? std::min(grid, resident<LOGS, DEL, CNT, L::SHORT, Loc>()) : grid;
+  k_rebuild<LOGS, DEL, CNT, L::SHORT, Loc><<<g1, 256, L::BYTES, st>>>(loc, p, parity,
+                                                                      use_list ? kFromList : kFromGrid, status);
+  count_launch();
+  const uint32_t g2 = std::min(grid, resident<LOGS, DEL, CNT, L::WIN, Loc>());
+  k_rebuild<LOGS, DEL, CNT, L::WIN, Loc><<<g2, 256, L::BYTES, st>>>(loc, p, parity, kFromRetry, status);
+  count_launch();
 }
 
 template <int LOGS, class Loc>
@@ -756,16 +797,15 @@ cudaError_t run_phases(const Loc& loc, const Partition& p, Op op, uint32_t spars
                        cudaStream_t st) {
   const bool cnt = p.counts != nullptr;
   if (op == Op::kDelete && cnt) return cudaErrorInvalidValue;  // deletes carry no counts
-  if (op == Op::kDelete) configure<LOGS, true, false, Loc>();
-  else if (cnt) configure<LOGS, false, true, Loc>();
-  else configure<LOGS, false, false, Loc>();
   const uint32_t half = (p.nregions + 1) / 2;
   for (int parity = 0; parity < 2; parity++) {
     uint32_t grid = parity ? p.nregions / 2 : half;
     if (!grid) continue;
     const int use_list = sparse_max != 0;
+    cudaError_t e = cudaMemsetAsync(p.retry, 0, 2 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
     if (use_list) {
-      cudaError_t e = cudaMemsetAsync(p.cursor, 0, 2 * sizeof(uint32_t), st);
+      e = cudaMemsetAsync(p.cursor, 0, 2 * sizeof(uint32_t), st);
       if (e != cudaSuccess) return e;
       const uint32_t sg = (grid + 127) / 128;
       if (op == Op::kDelete)
@@ -776,19 +816,11 @@ cudaError_t run_phases(const Loc& loc, const Partition& p, Op op, uint32_t spars
         k_sparse<LOGS, false, false, Loc><<<sg, 128, 0, st>>>(loc, p, parity, sparse_max, status);
       count_launch();
     }
-    // a persistent grid: as many CTAs as fit at once, or as regions exist
-    if (op == Op::kDelete) {
-      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, true, false, Loc>()) : grid;
-      k_rebuild<LOGS, true, false, Loc><<<pg, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, use_list, status);
-    } else if (cnt) {
-      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, false, true, Loc>()) : grid;
-      k_rebuild<LOGS, false, true, Loc><<<pg, 256, Lay<LOGS, true>::BYTES, st>>>(loc, p, parity, use_list, status);
-    } else {
-      const uint32_t pg = use_list ? std::min(grid, resident<LOGS, false, false, Loc>()) : grid;
-      k_rebuild<LOGS, false, false, Loc><<<pg, 256, Lay<LOGS, false>::BYTES, st>>>(loc, p, parity, use_list,
-                                                                                   status);
-    }
-    count_launch();
+    // persistent grids over lists: as many CTAs as fit at once, or as
+    // regions exist
+    if (op == Op::kDelete) launch_passes<LOGS, true, false>(loc, p, parity, use_list, grid, status, st);
+    else if (cnt) launch_passes<LOGS, false, true>(loc, p, parity, use_list, grid, status, st);
+    else launch_passes<LOGS, false, false>(loc, p, parity, use_list, grid, status, st);
   }
   return cudaGetLastError();
 }

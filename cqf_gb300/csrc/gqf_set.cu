@@ -261,7 +261,7 @@ int gqf_set_create(uint32_t n, const int* nbits, uint64_t max_batch_keys, gqf_se
               ok(cudaMemset(s->aux, 0, 256), "cudaMemset aux") &&
               ok(cudaMalloc((void**)&s->dqfs, n * sizeof(quotient_filter)), "cudaMalloc descriptors") &&
               ok(cudaMalloc((void**)&s->region_base, (n + 1) * sizeof(uint32_t)), "cudaMalloc region table") &&
-              ok(cudaMalloc((void**)&tables, 4 * cap * sizeof(uint32_t)), "cudaMalloc region arrays") &&
+              ok(cudaMalloc((void**)&tables, 5 * cap * sizeof(uint32_t)), "cudaMalloc region arrays") &&
               ok(cudaMalloc((void**)&s->part.keys, max_batch_keys * sizeof(uint32_t)), "cudaMalloc keys");
   if (good) {
     uint64_t at = 0;
@@ -275,6 +275,7 @@ int gqf_set_create(uint32_t n, const int* nbits, uint64_t max_batch_keys, gqf_se
     s->part.region_start = tables + cap;
     s->part.cursor = tables + 2 * cap;
     s->part.deferred = tables + 3 * cap;
+    s->part.retry = tables + 4 * cap;
     s->part.stats = reinterpret_cast<unsigned long long*>(s->aux + 128);
     good = good && layout_regions(s, kMinLogRegion);
   }

@@ -144,9 +144,9 @@ int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* r
  * allocator.  The batch is partitioned into one fixed array of
  * GQF_NOALLOC_SCRATCH_BYTES inside the library's device image, held by every
  * GPU that loads the library: a batch may hold at most
- *   (GQF_NOALLOC_SCRATCH_BYTES - 16 * (nslots / 2^region_log + 2), rounded up
+ *   (GQF_NOALLOC_SCRATCH_BYTES - 20 * (nslots / 2^region_log + 2), rounded up
  *    to 256) / 4 keys
- * (about 4.06 million at 2^28 slots); larger batches are refused with -1 and
+ * (about 4.03 million at 2^28 slots); larger batches are refused with -1 and
  * a message in gqf_last_error.  The first call on each device, with that
  * device current, looks up the array's address: make it before any stream
  * capture.  All calls share the array, so calls that overlap on the GPU race
