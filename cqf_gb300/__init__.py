@@ -319,9 +319,9 @@ class QF:
         return int(s.value)
 
     def counters(self) -> dict:
-        c = np.zeros(2, dtype=np.uint64)
-        self._ok(self.L.gqf_get_counters(self.h, c.ctypes.data, 2))
-        return {"deferred_regions": int(c[0]), "serial_keys": int(c[1])}
+        c = np.zeros(3, dtype=np.uint64)
+        self._ok(self.L.gqf_get_counters(self.h, c.ctypes.data, 3))
+        return {"deferred_regions": int(c[0]), "serial_keys": int(c[1]), "full_window_regions": int(c[2])}
 
     def clear_status(self):
         self._ok(self.L.gqf_clear_status(self.h))

@@ -567,17 +567,17 @@ int gqf_clear_status(QF* qf) {
   HostFilter* f = lookup(qf);
   if (!f) return -1;
   return ck(cudaMemsetAsync(status_ptr(f), 0, 4, f->stream), "memset status") &&
-         ck(cudaMemsetAsync(stats_ptr(f), 0, 16, f->stream), "memset counters") ? 0 : -1;
+         ck(cudaMemsetAsync(stats_ptr(f), 0, 24, f->stream), "memset counters") ? 0 : -1;
 }
 
 int gqf_get_counters(QF* qf, uint64_t* counters, int n) {
   HostFilter* f = lookup(qf);
   if (!f || !counters || n < 0) return -1;
-  unsigned long long c[2] = {0, 0};
-  if (!ck(cudaMemcpyAsync(c, stats_ptr(f), 16, cudaMemcpyDeviceToHost, f->stream), "memcpy counters") ||
+  unsigned long long c[3] = {0, 0, 0};
+  if (!ck(cudaMemcpyAsync(c, stats_ptr(f), 24, cudaMemcpyDeviceToHost, f->stream), "memcpy counters") ||
       !ck(cudaStreamSynchronize(f->stream), "sync"))
     return -1;
-  for (int i = 0; i < n && i < 2; i++) counters[i] = c[i];
+  for (int i = 0; i < n && i < 3; i++) counters[i] = c[i];
   return 0;
 }
 

@@ -33,7 +33,8 @@ struct Partition {
   uint32_t* cursor;        // nregions
   uint32_t* deferred;      // [0] = n, then region ids
   uint32_t* retry;         // nregions + 2: [0] = n, [1] = next taken, then region ids
-  unsigned long long* stats;  // [0] regions deferred, [1] keys applied serially (or nullptr)
+  unsigned long long* stats;  // [0] regions deferred, [1] keys applied serially, [2] regions retried in
+                              // the full window (or nullptr)
   uint32_t nregions;
   int log_region;          // a region is 2^log_region quotients
 };

@@ -626,6 +626,7 @@ __global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc 
     if (kShort) {
       const uint32_t at = atomicAdd(&p.retry[kListCount], 1u);
       p.retry[kListBase + at] = R;
+      if (p.stats) atomicAdd(&p.stats[2], 1ULL);
     } else {
       const uint32_t at = atomicAdd(&p.deferred[0], 1u);
       p.deferred[1 + at] = R;

@@ -304,8 +304,11 @@ int gqf_get_status(QF* qf, uint32_t* status);
 int gqf_clear_status(QF* qf);
 
 /* Counters since the last gqf_clear_status: [0] regions whose rebuild window
- * was exceeded (applied by the serial path), [1] keys applied serially.
- * Writes min(n, 2) values; synchronises the filter's stream. */
+ * was exceeded (applied by the serial path), [1] keys applied serially,
+ * [2] regions rebuilt in the full window (the region plus 2048 slots, 1024
+ * for 2048-quotient regions) because the first window (the region plus 256
+ * slots) could not hold their changes.  Writes min(n, 3) values;
+ * synchronises the filter's stream. */
 int gqf_get_counters(QF* qf, uint64_t* counters, int n);
 
 /* Empty the filter (asynchronous). */

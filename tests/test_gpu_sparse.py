@@ -128,3 +128,39 @@ def test_sparse_region_past_its_window_is_deferred(gq):
         assert qf.counters()["deferred_regions"] > before
         a, b = o.dump(), qf.export()
         assert np.array_equal(a, b), first_diff(a, b)
+
+
+@pytest.mark.parametrize("lr", [11, 12, 13])
+def test_region_past_its_short_window_takes_the_full_one(gq, lr):
+    """A cluster that runs 500 slots past its region: the first rebuild
+    window (the region plus 256 slots) cannot hold the shift, the full one
+    (plus 2048, or 1024 for 2048-quotient regions) can; the region is retried
+    there, not left to the serial pass, and the filter matches the oracle
+    after the insert and after the delete that shifts the cluster back."""
+    nbits = 16
+    reg = 1 << lr
+    rng = np.random.default_rng(lr)
+    q = np.arange(reg - 200, reg + 500, dtype=np.uint64)  # one key per slot, no gaps
+    fill = (q << np.uint64(8)) | rng.integers(0, 256, size=q.size).astype(np.uint64)
+    extra = (np.arange(reg - 180, reg - 170, dtype=np.uint64) << np.uint64(8)) | np.uint64(7)
+    o = oracle.Oracle(nbits)
+    o.bulk_insert(fill, key_is_hash=True)
+    flags = gq.QF_NO_LOCK | gq.QF_KEY_IS_HASH
+    with gq.QF(nbits, log_region=lr) as qf:
+        qf.set_sparse_max(0)
+        qf.bulk_insert(dev(fill), flags=flags)
+        c0 = qf.counters()
+        o.bulk_insert(extra, key_is_hash=True)
+        qf.bulk_insert(dev(extra), flags=flags)
+        c1 = qf.counters()
+        assert c1["full_window_regions"] > c0["full_window_regions"]
+        assert c1["deferred_regions"] == c0["deferred_regions"]
+        a, b = o.dump(), qf.export()
+        assert np.array_equal(a, b), first_diff(a, b)
+        o.bulk_delete(extra, key_is_hash=True)
+        qf.bulk_delete(dev(extra), flags=flags)
+        c2 = qf.counters()
+        assert c2["full_window_regions"] > c1["full_window_regions"]
+        assert c2["deferred_regions"] == c0["deferred_regions"]
+        a, b = o.dump(), qf.export()
+        assert np.array_equal(a, b), first_diff(a, b)
