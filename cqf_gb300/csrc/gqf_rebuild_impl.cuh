@@ -107,6 +107,47 @@ struct Img {
 template <bool DEL, bool WRITE>
 __device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* keys, const uint32_t* cnts,
                          int ki, int kj, Img out, int pos) {
+  if (!cnts && kj == ki + 1) {  // one key, counted once: the common case
+    const int r = (int)(keys[ki] & 255u);
+    if (!has_old) {
+      if (DEL) return 0;
+      if (WRITE) out.slot(pos) = (uint8_t)r;
+      return 1;
+    }
+    // Remainders that strictly increase along the run are all counted once
+    // (a counter of two or more repeats its remainder or steps down after
+    // it), so the key only adds or drops one slot.
+    int prev = -1, at = -1, ins = e + 1;
+    bool single = true;
+    for (int t = s; t <= e; t++) {
+      const int v = cur.slot(t);
+      if (v <= prev) { single = false; break; }
+      if (v == r) at = t;
+      if (v > r && ins > e) ins = t;
+      prev = v;
+    }
+    if (single && (DEL || at < 0)) {
+      const int len = e - s + 1;
+      if (DEL && at < 0) {  // not in the run: nothing changes
+        if (WRITE)
+          for (int t = 0; t < len; t++) out.slot(pos + t) = cur.slot(s + t);
+        return len;
+      }
+      if (DEL) {
+        if (WRITE)
+          for (int t = s, o = pos; t <= e; t++)
+            if (t != at) out.slot(o++) = cur.slot(t);
+        return len - 1;
+      }
+      if (WRITE) {
+        int o = pos;
+        for (int t = s; t < ins; t++) out.slot(o++) = cur.slot(t);
+        out.slot(o++) = (uint8_t)r;
+        for (int t = ins; t <= e; t++) out.slot(o++) = cur.slot(t);
+      }
+      return len + 1;
+    }
+  }
   auto get = [&](uint64_t i) -> uint64_t { return cur.slot((int)i); };
   auto end = [&](uint64_t i) -> int { return cur.is_end((int)i); };
   const uint64_t lim = (uint64_t)e + 1;  // the walk never leaves the run [s, e]
