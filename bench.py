@@ -835,6 +835,7 @@ def run_serving(args, torch, cqf_gb300):
         pool[a:b].copy_(synth._splitmix_range_dev(12, a, b, "cuda"))
     out_cap = 1 << 28
     outbuf = torch.empty(out_cap, dtype=torch.int64, pin_memory=True)
+    outbuf.copy_(torch.zeros(out_cap, dtype=torch.int64, device="cuda"))  # first device writes, untimed
     torch.cuda.synchronize()
 
     def payload(r):
@@ -846,7 +847,8 @@ def run_serving(args, torch, cqf_gb300):
         s0 = max(0, ins - n // 2)
         return pool[s0:s0 + n], (max(dele, s0) - s0, ins - s0)
 
-    def run(realtime_rate=None):
+    def run(realtime_rate=None, nreq=None):
+        reqs = st.reqs if nreq is None else st.reqs[:nreq]
         qf = cqf_gb300.QF(nbits)
         srv = cqf_gb300.Server(qf)
         ops = {"get": cqf_gb300.OP_GET, "insert": cqf_gb300.OP_INSERT, "delete": cqf_gb300.OP_DELETE}
@@ -876,7 +878,7 @@ def run_serving(args, torch, cqf_gb300):
         t0 = time.perf_counter()
         sched = 0.0
         lag = 0.0
-        for seq, r in enumerate(st.reqs):
+        for seq, r in enumerate(reqs):
             kind, n = r[0], r[1]
             if realtime_rate:
                 sched += r[2] / realtime_rate
@@ -906,13 +908,14 @@ def run_serving(args, torch, cqf_gb300):
         srv.close()
         qf.close()
         lat_sorted = np.sort(np.array(lat))
-        return {"seconds": dt, "mkeys_s": st.total_keys / dt / 1e6,
+        return {"seconds": dt, "mkeys_s": sum(r[1] for r in reqs) / dt / 1e6,
                 "p50_ms": float(np.percentile(lat_sorted, 50)), "p99_ms": float(np.percentile(lat_sorted, 99)),
                 "max_ms": float(lat_sorted[-1]), "launches": int(stats["launches"]),
                 "peak_staging_gb": stats["peak_staging_bytes"] / 1e9, "staging_gb": stats["staging_bytes"] / 1e9,
                 "submit_lag_max_ms": lag * 1e3, "present_found": checks["ok"],
                 "gets_checked": checks["checked"]}
 
+    run(None, 64)  # warm-up on a fresh filter and server, untimed
     sat = run(None)
     rate = args.serve_load * sat["mkeys_s"] * 1e6 / st.mean_size  # requests per second
     pois = run(rate)
@@ -943,6 +946,8 @@ def run_serving_ref(st, nbits, pool, rate, torch):
     dbuf = torch.empty(1 << 24, dtype=torch.int64, device="cuda")
     dout = torch.empty(1 << 24, dtype=torch.int64, device="cuda")
     hout = torch.empty(1 << 24, dtype=torch.int64, pin_memory=True)
+    dout.zero_()
+    hout.copy_(dout)  # first device writes to the pinned buffer, untimed (as for our arm)
     service = []
     try:
         for kind, n, _, arg in st.reqs:
