@@ -37,7 +37,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "bulk insert/get Mkeys/s at 2^28 slots 90% load vs ref CUDA; serving p99 ms"
 UNIT = "Mkeys/s"
-# algorithmic bytes per key (reference packed format)
+# Algorithmic bytes, counted on the reference's packed format (81-byte
+# blocks: 1-byte offset, occupieds, runends, 64 one-byte slots).  A get moves
+# its key, its count and one block; a bulk insert or delete reads and writes
+# every block its batch touches once, plus its keys through the partition.
 BYTES_GET = 97.0          # 8 key in + 8 count out + one 81-byte block
 BLOCK_BYTES = 81.0
 PART_BYTES_PER_KEY = 16.0  # key read + partitioned key written
