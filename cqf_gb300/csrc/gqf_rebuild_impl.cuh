@@ -655,7 +655,7 @@ enum : int { kFromGrid = 0, kFromList = 1, kFromRetry = 2 };
 // hold, and those whose keys need several rounds (they may grow further);
 // the full pass leaves what it cannot hold to the serial fallback.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
-__global__ void __launch_bounds__(256, CNT ? 2 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
+__global__ void __launch_bounds__(256, CNT ? 3 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
                                                                              int from, uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr bool kShort = SPAN < L::WIN;
