@@ -10,8 +10,11 @@
 //
 //   * one CTA per region of 2^LOGS quotients, even regions then odd ones (the
 //     reference's schedule), so two CTAs never touch the same slots;
-//   * the CTA stages a window of LOGS-region + PUSH slots in shared memory
-//     (the region plus the head of the next one, which its growth may push);
+//   * the CTA stages a window in shared memory: the region plus the head of
+//     the next one, which its growth may push.  A first launch per parity
+//     uses a short head (TAIL slots), enough for almost every region; a
+//     second launch takes the regions it could not hold with the full head
+//     (PUSH slots);
 //   * it groups the region's new keys by quotient with a counting sort in
 //     shared memory, merges them with the old counters of the touched runs
 //     only (decode_counter / encode_counter, src/gqf.cu:1216-1345), and
@@ -20,8 +23,8 @@
 //   * untouched runs move byte-parallel (every slot knows its run's shift);
 //   * it writes back only the blocks that changed.
 //
-// A rebuild whose changes would reach past the window (a cluster longer than
-// PUSH slots, or the end of the table) is deferred: nothing is written and the
+// A rebuild whose changes would reach past the full window (a cluster longer
+// than PUSH slots, or the end of the table) is deferred: nothing is written and the
 // region is applied afterwards by a single-thread serial pass built from the
 // reference's own single-key algorithms (gqf_device.cuh), which handles any
 // cluster length and reports a full table like the reference does.
