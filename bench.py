@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "bulk insert/get Mkeys/s at 2^28 slots 90% load vs ref CUDA; serving p99 ms"
 UNIT = "Mkeys/s"
+L2_BYTES = 129 * 2**20  # GB300 L2
 # Algorithmic bytes, counted on the reference's packed format (81-byte
 # blocks: 1-byte offset, occupieds, runends, 64 one-byte slots).  A get moves
 # its key, its count and one block; a bulk insert or delete reads and writes
@@ -87,6 +88,14 @@ class Workload:
     def touched_blocks(self, b):
         return self.nblocks * (1.0 - np.exp(-b / self.nblocks))
 
+    def l2_note(self):
+        keys, filt = 8 * (self.n_insert + self.n_get), 96 * self.nblocks
+        size = lambda b: f"{b / 1e9:.2g} GB" if b >= 1e9 else f"{b / 1e6:.3g} MB"
+        what = f"inputs ({size(keys)} of keys, {size(filt)} filter)"
+        if keys + filt > L2_BYTES:
+            return what + " exceed the 129 MB L2; no extra flush"
+        return what + " fit the 129 MB L2"
+
     def describe(self):
         return {
             "workload": f"config 2: nbits={self.nbits} ({self.nslots} slots), fill 90% ({self.n_insert} keys) "
@@ -100,7 +109,7 @@ class Workload:
             "deletes": self.n_get,
             "key_ops_per_step": self.key_ops,
             "keys": "splitmix64 seed 1 (present), seed 2 (absent)",
-            "l2": "inputs (1.9 GB of keys, 0.4 GB filter) exceed the 129 MB L2; no extra flush",
+            "l2": self.l2_note(),
         }
 
 
