@@ -8,6 +8,7 @@
 //   * no per-call device allocation (thrust temporaries, managed memory):
 //     partition scratch is owned by the filter and grown stream-ordered;
 //   * the filter is built on the device (memset), not on the host and copied.
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -112,8 +113,8 @@ HostFilter* lookup(const QF* qf) {
 }
 
 int auto_log_region(int nbits) {
-  // 2^12-quotient regions fit three rebuild CTAs per SM; small tables use
-  // 2^11 for more regions per phase.
+  // 2^12-quotient regions fit four rebuild CTAs per SM and measured fastest
+  // on large tables; small tables use 2^11 for more regions per phase.
   return nbits >= 21 ? 12 : 11;
 }
 
@@ -158,14 +159,19 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
     return false;
   }
   if (nkeys > f->key_cap || (with_counts && !f->counts_alloc)) {
-    uint64_t cap = nkeys > f->key_cap ? nkeys + nkeys / 8 + 1024 : f->key_cap;
+    const uint64_t cap = nkeys > f->key_cap ? nkeys + nkeys / 8 + 1024 : f->key_cap;
+    const bool had_counts = f->counts_alloc;
     if (f->part.keys) cudaFreeAsync(f->part.keys, st);
     if (f->part.counts) cudaFreeAsync(f->part.counts, st);
+    // until both allocations succeed the filter holds no key scratch, so a
+    // failed growth is retried by the next call instead of reused
     f->part.keys = nullptr;
     f->part.counts = nullptr;
+    f->key_cap = 0;
+    f->counts_alloc = false;
     if (!ck(cudaMallocAsync((void**)&f->part.keys, cap * sizeof(uint32_t), st), "cudaMallocAsync keys"))
       return false;
-    if (with_counts || f->counts_alloc) {
+    if (with_counts || had_counts) {
       if (!ck(cudaMallocAsync((void**)&f->part.counts, cap * sizeof(uint32_t), st), "cudaMallocAsync counts"))
         return false;
       f->counts_alloc = true;
@@ -175,6 +181,8 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
   if (nr + 2 > f->region_cap) {
     uint32_t cap = nr + 2;
     if (f->part.region_count) cudaFreeAsync(f->part.region_count, st);
+    f->part.region_count = f->part.region_start = f->part.cursor = f->part.deferred = f->part.retry = nullptr;
+    f->region_cap = 0;
     uint32_t* base = nullptr;
     // region_count | region_start | cursor | deferred | retry, one allocation
     if (!ck(cudaMallocAsync((void**)&base, 5ULL * cap * sizeof(uint32_t), st), "cudaMallocAsync regions"))
