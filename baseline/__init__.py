@@ -17,7 +17,10 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"
+# The reference tree: $GQF_REFERENCE_TREE, else a checkout named "reference"
+# beside this repository.
+REFERENCE_TREE = os.environ.get("GQF_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                       "reference")
 CCCL = "/usr/local/cuda/include/cccl"
 
 

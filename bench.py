@@ -10,6 +10,7 @@ step (inserts + gets + deletes), in Mkeys/s; per-operation rates are reported
 beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --case insert|delete|get|zipf|kmers [--nbits B] [--load F] [--extra E]
 
 --impl ours (default) prints one JSON line with the device-resident value,
 the end-to-end value through the C ABI from pinned host buffers (copies in
@@ -18,6 +19,19 @@ clocks sampled during the timed region and the number of library kernel
 launches.  --impl reference times the reference's CPU implementation of the
 same path (the oracle restatement, multi-threaded over regions the way the
 reference's launch is) on the host cores.
+
+--case runs one workload on one filter for profiling a kernel in isolation
+(no JSON contract line): it fills a 2^nbits-slot filter with splitmix64 keys
+(seed 1) in batches of --case-batch keys up to --load of its slots, then runs
+--extra more batches of the op (insert: fresh keys; delete / get: keys the
+fill inserted) and prints one line of CUDA-event times.  zipf and kmers
+instead run --extra counted inserts on an empty filter: 2^28 Zipf(1.5) draws
+over 2^24 keys through bulk_insert_reduce, or the canonical 31-mers of 2^20
+synthetic 150-base reads through the device k-mer counter (--load and
+--case-batch do not apply).  Each bulk insert or delete launches, per parity
+of regions, the short-window and the full-window rebuild, so the k-th rebuild
+launch of the extra batches is number 4 * (fill calls) + k; the fill makes
+ceil(load * 2^nbits / case-batch) calls.
 """
 from __future__ import annotations
 
@@ -67,6 +81,11 @@ def parse():
     ap.add_argument("--serve-nbits", type=int, default=30)
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="Poisson offered load as a fraction of the measured saturated throughput")
+    ap.add_argument("--case", choices=["insert", "delete", "get", "zipf", "kmers"], default=None,
+                    help="profile one op on one filter instead of the benchmark")
+    ap.add_argument("--load", type=float, default=0.8, help="--case: fill fraction of the slots")
+    ap.add_argument("--case-batch", type=int, default=1 << 24, help="--case: keys per bulk call")
+    ap.add_argument("--extra", type=int, default=1, help="--case: bulk calls after the fill")
     return ap.parse_args()
 
 
@@ -1070,7 +1089,7 @@ def run_reference(args, wl, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic (splitmix64 keys)",
-        "config": wl.describe(),
+        "config": wl.describe() | {"parallelism": "replicas" if world > 1 else "single GPU"},
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"each step is the full workload ({wl.key_ops} key ops) on {threads} threads"},
@@ -1078,8 +1097,78 @@ def run_reference(args, wl, rank, world):
     }
 
 
+# ------------------------------------------------- single-kernel profiling
+
+def run_case(a):
+    """--case: one fill and a few bulk calls on one filter (see the module
+    docstring); prints one JSON line of CUDA-event times."""
+    import math
+
+    import torch
+
+    import cqf_gb300
+    from cqf_gb300 import build, synth
+
+    build.build()
+    if a.case in ("zipf", "kmers"):
+        if a.case == "zipf":
+            data = synth.zipf_keys_dev(3, 1 << 28, 1 << 24)
+        else:
+            data = synth.dna_reads_dev(4, 1 << 20, 150, 1 << 24, 0.01)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        out = {"nbits": a.nbits, "op": a.case, "calls": a.extra, "ms": []}
+        with cqf_gb300.QF(a.nbits) as qf:
+            for _ in range(a.extra):
+                qf.reset()
+                e0.record()
+                if a.case == "zipf":
+                    qf.bulk_insert_reduce(data)
+                else:
+                    qf.bulk_insert_kmers(data, 31)
+                e1.record()
+                torch.cuda.synchronize()
+                out["ms"].append(round(e0.elapsed_time(e1), 3))
+            out["status"] = qf.status()
+            out["counters"] = qf.counters()
+        return out
+    B = a.case_batch
+    n_fill = int(a.load * (1 << a.nbits))
+    n_extra = a.extra * B
+    keys = synth.splitmix64_dev(1, n_fill + (n_extra if a.case == "insert" else 0))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"nbits": a.nbits, "load": a.load, "batch": B, "op": a.case, "fill_calls": math.ceil(n_fill / B)}
+    with cqf_gb300.QF(a.nbits) as qf:
+        e0.record()
+        for s in range(0, n_fill, B):
+            qf.bulk_insert(keys[s:min(s + B, n_fill)])
+        e1.record()
+        torch.cuda.synchronize()
+        out["fill_ms"] = round(e0.elapsed_time(e1), 3)
+        res = torch.empty(B, dtype=torch.int64, device="cuda")
+        e0.record()
+        for i in range(a.extra):
+            if a.case == "insert":
+                qf.bulk_insert(keys[n_fill + i * B:n_fill + (i + 1) * B])
+            else:
+                s = (i * B) % max(1, n_fill - B)
+                chunk = keys[s:s + B]
+                if a.case == "delete":
+                    qf.bulk_delete(chunk)
+                else:
+                    qf.bulk_get(chunk, res)
+        e1.record()
+        torch.cuda.synchronize()
+        out["extra_ms"] = round(e0.elapsed_time(e1), 3)
+        out["status"] = qf.status()
+        out["counters"] = qf.counters()
+    return out
+
+
 def main():
     args = parse()
+    if args.case:
+        print(json.dumps(run_case(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     wl = Workload(args.nbits, args.batch_log, args.get_log)

@@ -45,6 +45,7 @@ struct HostFilter {
   quotient_filter h{};      // host mirror of the descriptor
   Geom g{};
   cudaStream_t stream = 0;  // legacy default stream, like the reference
+  int device = 0;           // the device the filter's memory lives on
   int log_region = 12;
   bool auto_region = true;
   uint32_t sparse_max = GQF_SPARSE_AUTO;  // regions with <= this many keys go key by key
@@ -294,7 +295,13 @@ bool internal_view(const QF* qf, FilterView* v) {
   v->nregions = nregions_for(f, f->log_region);
   v->stream = f->stream;
   v->mu = &f->mu;
+  v->device = f->device;
   return true;
+}
+
+uint32_t internal_sparse_max(const QF* qf, uint64_t n) {
+  HostFilter* f = lookup(qf);
+  return f ? sparse_max_for(f, n) : kDefaultSparseMax;
 }
 
 void internal_set_error(const char* msg) { set_err(msg); }
@@ -324,6 +331,7 @@ void qf_malloc_device(QF** qf, int nbits, bool bulk_config) {
   h.key_bits = (uint32_t)nbits + 8;
   h.nlocks = h.xnslots / kLockRegion + 2;  // num_locks, src/gqf.cu:1996
   h.lock_spin_limit = 1u << 20;
+  f->device = current_device();
   bool ok = ck(cudaMalloc((void**)&h.blocks, h.nblocks * sizeof(Block)), "cudaMalloc blocks") &&
             ck(cudaMemset(h.blocks, 0, h.nblocks * sizeof(Block)), "cudaMemset blocks") &&
             ck(cudaMalloc((void**)&h.locks, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMalloc locks") &&

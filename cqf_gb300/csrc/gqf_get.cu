@@ -50,13 +50,7 @@ __global__ void __launch_bounds__(256) k_bulk_get_misses(Geom g, const uint64_t*
 }
 
 int grid_for(uint64_t n) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
+  const int sms = sm_count();
   uint64_t want = (n + 255) / 256;
   uint64_t cap = (uint64_t)sms * 32;
   if (want > cap) want = cap;

@@ -113,17 +113,6 @@ __global__ void __launch_bounds__(256) k_pair_probe(Geom mem, const uint64_t* __
   }
 }
 
-int sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
-  return sms;
-}
-
 }  // namespace
 
 cudaError_t launch_enum_count(const Geom& g, uint32_t* per_block, cudaStream_t st) {

@@ -14,6 +14,36 @@ namespace gqf {
 extern std::atomic<unsigned long long> g_launches;
 inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Launch geometry and kernel attributes (the dynamic shared-memory limit set
+// by cudaFuncSetAttribute) belong to one device, so every cache of them is
+// kept per device, indexed by the current device.
+constexpr int kMaxDevices = 64;
+inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) d = 0;
+  return d;
+}
+// SMs of the current device.
+inline int sm_count() {
+  static std::atomic<int> sms[kMaxDevices];
+  const int d = current_device();
+  int v = sms[d].load(std::memory_order_relaxed);
+  if (!v) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || v <= 0) v = 152;
+    sms[d].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+// Runs set_up() once per device for the cache `flags` (one array per kernel
+// or kernel variant).
+template <class F>
+inline void once_per_device(std::atomic<bool>* flags, F&& set_up) {
+  const int d = current_device();
+  if (flags[d].load(std::memory_order_acquire)) return;
+  set_up();
+  flags[d].store(true, std::memory_order_release);
+}
+
 // Geometry of one filter as passed by value to kernels.
 struct Geom {
   Block* blocks;
@@ -97,8 +127,11 @@ struct FilterView {
   uint32_t nregions;
   cudaStream_t stream;
   void* mu;  // std::mutex* serialising calls on the filter
+  int device;  // the device holding the filter's memory
 };
 bool internal_view(const quotient_filter* qf, FilterView* v);
+// The key-by-key threshold bulk_insert uses for a batch of n keys on qf.
+uint32_t internal_sparse_max(const quotient_filter* qf, uint64_t n);
 void internal_set_error(const char* msg);
 
 // Region sizes the rebuild kernel is instantiated for.

@@ -9,6 +9,12 @@
 // point instead partitions the batch into one fixed array in the library's own
 // device image, so it never allocates.
 //
+// Apart from where its scratch lives it is bulk_insert: the same partition and
+// rebuild kernels, the same key-by-key threshold (gqf_set_sparse_max).  Its
+// stream is the one passed in, NULL meaning the legacy default stream (as for
+// the other *_async calls), not the filter's stream from gqf_set_stream.  The
+// current device must be the one the filter was created on.
+//
 // The array (GQF_NOALLOC_SCRATCH_BYTES) is a file-scope __device__ variable:
 // every GPU that loads the library holds it until the process exits.  Host
 // code cannot use the variable's name as a device address, so the first call
@@ -28,9 +34,8 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GQF_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+void* g_scratch_addr[gqf::kMaxDevices] = {nullptr};
 
 }  // namespace
 
@@ -43,6 +48,16 @@ extern "C" int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* k
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     internal_set_error("gqf_bulk_insert_noalloc: no usable current device");
+    return -1;
+  }
+  // The scratch address and the kernels' attributes belong to the current
+  // device; the filter's memory lives on the device it was created on.
+  if (dev != v.device) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg,
+                  "gqf_bulk_insert_noalloc: the current device is %d but the filter lives on device %d; "
+                  "make that device current first", dev, v.device);
+    internal_set_error(msg);
     return -1;
   }
   void* base = nullptr;
@@ -102,7 +117,8 @@ extern "C" int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* k
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int key_is_hash = (flags & QF_KEY_IS_HASH) ? 1 : 0;
   cudaError_t e = launch_partition(v.g, p, keys, nvals, key_is_hash, v.status, st);
-  if (e == cudaSuccess) e = launch_rebuild(v.g, p, Op::kInsert, v.dqf, v.status, st);
+  if (e == cudaSuccess)
+    e = launch_rebuild(v.g, p, Op::kInsert, v.dqf, v.status, st, internal_sparse_max(qf, nvals));
   if (e != cudaSuccess) {
     char msg[160];
     std::snprintf(msg, sizeof msg, "gqf_bulk_insert_noalloc: %s", cudaGetErrorString(e));

@@ -154,13 +154,7 @@ __global__ void __launch_bounds__(256) k_part_scatter(Geom g, const uint64_t* __
 }
 
 int grid_for(uint64_t n) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
+  const int sms = sm_count();
   uint64_t want = (n + 255) / 256;
   uint64_t cap = (uint64_t)sms * 16;
   if (want > cap) want = cap;

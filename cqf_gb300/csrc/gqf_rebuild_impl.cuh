@@ -795,29 +795,33 @@ __global__ void k_fallback(Loc loc, Partition p, int del, uint32_t* status) {
   }
 }
 
+// The shared-memory limit is an attribute of the kernel on one device: set
+// it once per instantiation and device.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 void configure() {
-  static bool done = false;  // per instantiation
-  if (done) return;
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       Lay<LOGS, CNT>::BYTES);
-  cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  done = true;
+  static std::atomic<bool> done[kMaxDevices];
+  once_per_device(done, [] {
+    cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         Lay<LOGS, CNT>::BYTES);
+    cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
+  });
 }
 
-// CTAs of k_rebuild resident at once on the device.
+// CTAs of k_rebuild resident at once on the current device.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 uint32_t resident() {
-  static uint32_t n = 0;  // per instantiation
-  if (!n) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static std::atomic<uint32_t> n[kMaxDevices];  // per instantiation and device
+  const int d = current_device();
+  uint32_t v = n[d].load(std::memory_order_relaxed);
+  if (!v) {
+    int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, 256,
                                                   Lay<LOGS, CNT>::BYTES);
-    n = (uint32_t)std::max(1, sms) * (uint32_t)std::max(1, per);
+    v = (uint32_t)std::max(1, sm_count()) * (uint32_t)std::max(1, per);
+    n[d].store(v, std::memory_order_relaxed);
   }
-  return n;
+  return v;
 }
 
 // The two passes of one parity: the short windows over the grid or the

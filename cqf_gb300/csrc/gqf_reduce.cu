@@ -327,27 +327,15 @@ __global__ void __launch_bounds__(kRegionThreads) k_merge_regions(Partition p, u
   }
 }
 
-int sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
-  return sms;
-}
-
 }  // namespace
 
 template <class Src>
 cudaError_t run_merge_tiles(const Src& src, uint64_t ntiles, uint64_t* out_hashes, uint32_t* out_counts,
                             unsigned long long* n_out, cudaStream_t st) {
-  static bool configured = false;  // per source type
-  if (!configured) {
+  static std::atomic<bool> configured[kMaxDevices];  // per source type and device
+  once_per_device(configured, [] {
     cudaFuncSetAttribute(k_merge_tiles<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-    configured = true;
-  }
+  });
   if (ntiles == 0) return cudaSuccess;
   const uint64_t cap = (uint64_t)sm_count() * 2;  // two 96 KB tables per SM
   const int grid = (int)(ntiles < cap ? ntiles : cap);
@@ -398,11 +386,10 @@ cudaError_t launch_kmers(const uint8_t* reads, uint64_t nreads, uint32_t read_le
 
 cudaError_t launch_merge_regions(const Partition& p, cudaStream_t st, const unsigned long long* n_merged,
                                  uint64_t n_in) {
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<bool> configured[kMaxDevices];
+  once_per_device(configured, [] {
     cudaFuncSetAttribute(k_merge_regions, cudaFuncAttributeMaxDynamicSharedMemorySize, kRegionSmem);
-    configured = true;
-  }
+  });
   if (!p.counts) return cudaErrorInvalidValue;
   const uint32_t limit = p.log_region >= 13 ? 4096u : 2048u;  // keys one rebuild round takes
   const uint32_t cap = (uint32_t)sm_count() * 3;

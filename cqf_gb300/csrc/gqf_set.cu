@@ -59,17 +59,6 @@ bool ok(cudaError_t e, const char* what) {
   return false;
 }
 
-int sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
-  return sms;
-}
-
 int grid_for_keys(uint64_t n) {
   uint64_t want = (n + 255) / 256, cap = (uint64_t)sm_count() * 16;
   return (int)std::max<uint64_t>(1, std::min(want, cap));

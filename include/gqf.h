@@ -140,17 +140,22 @@ int gqf_bulk_get_async(QF* qf, uint64_t nvals, const uint64_t* vals, uint64_t* r
  * allocate device memory while they run (a process whose device budget is
  * fixed at start-up, a plugin whose host framework owns all device memory, a
  * loop that cannot take cudaMalloc's implicit synchronisation).  Same result
- * as bulk_insert, on `stream` (NULL = legacy default stream); it calls no
- * allocator.  The batch is partitioned into one fixed array of
- * GQF_NOALLOC_SCRATCH_BYTES inside the library's device image, held by every
- * GPU that loads the library: a batch may hold at most
+ * as bulk_insert, with the same key-by-key threshold (gqf_set_sparse_max); it
+ * calls no allocator.  It runs on `stream`: NULL means the legacy default
+ * stream, as for the other *_async calls, not the filter's stream set by
+ * gqf_set_stream.  The current device must be the filter's own (the device
+ * current at qf_malloc_device); otherwise the call is refused with -1.  The
+ * batch is partitioned into one fixed array of GQF_NOALLOC_SCRATCH_BYTES
+ * inside the library's device image, held by every GPU that loads the
+ * library: a batch may hold at most
  *   (GQF_NOALLOC_SCRATCH_BYTES - 20 * (nslots / 2^region_log + 2), rounded up
  *    to 256) / 4 keys
- * (about 4.03 million at 2^28 slots); larger batches are refused with -1 and
- * a message in gqf_last_error.  The first call on each device, with that
- * device current, looks up the array's address: make it before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU race
- * and must be serialised by the caller.  Returns 0 on success. */
+ * (about 3.87 million at 2^28 slots with the default 2^12-quotient regions,
+ * 4.03 million with gqf_set_region_log 13); larger batches are refused with
+ * -1 and a message in gqf_last_error.  The first call on each device, with
+ * that device current, looks up the array's address: make it before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race and must be serialised by the caller.  Returns 0 on success. */
 #define GQF_NOALLOC_SCRATCH_BYTES (16u << 20)
 int gqf_bulk_insert_noalloc(QF* qf, uint64_t nvals, const uint64_t* keys, uint8_t flags, void* stream);
 

@@ -22,7 +22,10 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_LIB_PATH = os.path.join(REF_DIR, "libgqf_ref.so")
-REFERENCE_TREE = "/root/reference"
+# The reference tree: $GQF_REFERENCE_TREE, else a checkout named "reference"
+# beside this repository.  Only the build recipes read it.
+REFERENCE_TREE = os.environ.get("GQF_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                       "reference")
 
 _vp, _u64, _int = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
 
