@@ -36,6 +36,7 @@ ceil(load * 2^nbits / case-batch) calls.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -216,6 +217,34 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def sha256_of(a) -> str:
+    """SHA-256 of an array's bytes (a numpy array, or a torch tensor copied
+    to the host)."""
+    if hasattr(a, "cpu"):
+        a = a.cpu().numpy()
+    return hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).data).hexdigest()
+
+
+PARITY_KEYS = ("dump_insert", "counts_present", "counts_absent", "dump_delete")
+
+
+def parity_block(nbits, sides):
+    """Word-for-word agreement of the sides that ran the same step: the
+    packed filter after the inserts and after the deletes, and the count
+    arrays of the present and absent gets (equal absent counts = the same
+    false-positive set with the same counts)."""
+    sides = {k: v for k, v in sides.items() if isinstance(v, dict) and "dump_insert" in v}
+    out = {"nbits": nbits, "compared": sorted(sides)}
+    names = {"dump_insert": "dump_insert_equal", "counts_present": "counts_present_equal",
+             "counts_absent": "fp_set_equal", "dump_delete": "dump_delete_equal"}
+    for k in PARITY_KEYS:
+        vals = {s: d[k] for s, d in sides.items() if k in d}
+        out[names[k]] = len(vals) >= 2 and len(set(vals.values())) == 1
+    out["false_positives_absent"] = {s: d.get("false_positives") for s, d in sides.items()}
+    out["sha256"] = {s: {k: d[k] for k in PARITY_KEYS if k in d} for s, d in sides.items()}
+    return out
+
+
 def profile_traffic():
     """DRAM bytes per unit of work (probe, key or block) of each kernel from
     the committed ncu summaries (profiles/ncu_traffic.txt)."""
@@ -292,14 +321,26 @@ def run_gpu(args, wl, rank, world):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    # correctness of the last warm-up step, outside the timed region
+    # correctness of one whole step, outside the timed region: the packed
+    # filter after the inserts and after the deletes and both count arrays,
+    # hashed for the word-for-word comparison with the reference's CUDA build
+    # and the oracle
     qf.reset()
     for s, n in wl.batches:
         qf.bulk_insert(keys[s:s + n], n=n)
+    ours_par = {"dump_insert": sha256_of(qf.export())}
     qf.bulk_get(present, out)
     ok_present = bool((out > 0).all().item())
+    ours_par["counts_present"] = sha256_of(out)
     qf.bulk_get(absent, out)
     fp = int((out > 0).sum().item())
+    ours_par["counts_absent"] = sha256_of(out)
+    ours_par["false_positives"] = fp
+    for s in range(0, wl.n_get, wl.batch):
+        n = min(wl.batch, wl.n_get - s)
+        qf.bulk_delete(present[s:s + n], n=n)
+    ours_par["dump_delete"] = sha256_of(qf.export())
+    ours_par["status"] = qf.status()
     torch.cuda.synchronize()
 
     clocks = ClockSampler(torch.cuda.current_device())
@@ -393,13 +434,17 @@ def run_gpu(args, wl, rank, world):
         e2e = run_e2e(args, wl, qf, keys, absent, torch, dist, world)
 
     cpu = None
+    cpu_par = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = run_cpu_sample(wl, keys, absent, args)
+        cpu_par = cpu.pop("parity", None)
 
     ref_cuda = None
     if rank == 0 and world == 1 and not args.no_ref_cuda:
         qf.close()
         ref_cuda = run_ref_cuda(wl, keys, absent, ops, value, torch)
+    parity = parity_block(wl.nbits, {"ours": ours_par, "oracle": cpu_par,
+                                     "ref_cuda": (ref_cuda or {}).pop("parity", None)})
 
     workloads = {}
     if not args.no_skew and args.nbits == 28:
@@ -443,6 +488,7 @@ def run_gpu(args, wl, rank, world):
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches // args.steps),
         "check": {"present_all_found": ok_present, "false_positives_absent": fp, "status": status},
+        "parity": parity,
     }
     qf.close()
     if dist:
@@ -549,6 +595,7 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
     scratch = torch.empty(wl.batch, dtype=torch.int64, device="cuda")
     out = torch.empty(wl.n_get, dtype=torch.int64, device="cuda")
     t = {"insert": 0.0, "get": 0.0, "delete": 0.0}
+    par = {}  # hashes of its filter and counts, taken between the timed calls
     try:
         for s0, n in wl.batches:
             scratch[:n].copy_(keys[s0:s0 + n])
@@ -557,15 +604,18 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
             r.bulk_insert(scratch, n)
             torch.cuda.synchronize()
             t["insert"] += time.perf_counter() - a
-        for probe in (keys[: wl.n_get], absent):
+        par["dump_insert"] = sha256_of(r.dump())
+        for name, probe in (("counts_present", keys[: wl.n_get]), ("counts_absent", absent)):
             torch.cuda.synchronize()
             a = time.perf_counter()
             r.bulk_get(probe, out)
             torch.cuda.synchronize()
             t["get"] += time.perf_counter() - a
-        r.bulk_get(keys[: wl.n_get], out)
-        torch.cuda.synchronize()
-        found = bool((out > 0).all().item())
+            par[name] = sha256_of(out)
+            if name == "counts_present":
+                found = bool((out > 0).all().item())
+            else:
+                par["false_positives"] = int((out > 0).sum().item())
         for s0 in range(0, wl.n_get, wl.batch):
             n = min(wl.batch, wl.n_get - s0)
             scratch[:n].copy_(keys[s0:s0 + n])
@@ -574,6 +624,7 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
             r.bulk_delete(scratch, n)
             torch.cuda.synchronize()
             t["delete"] += time.perf_counter() - a
+        par["dump_delete"] = sha256_of(r.dump())
     finally:
         r.close()
     total = sum(t.values())
@@ -592,6 +643,7 @@ def run_ref_cuda(wl, keys, absent, ours_ops, ours_value, torch):
             "delete": round(ours_ops["delete"]["mkeys_s"] / rates["delete_mkeys_s"], 2),
         },
         "present_all_found": found,
+        "parity": par,
         "what": "reference src/gqf.cu kernels compiled for sm_103a from its sources; host orchestration "
                 "restated (baseline/refgpu.py), thrust::sort replaced by torch.sort",
     }
@@ -1023,25 +1075,38 @@ def run_cpu_sample(wl, keys_dev, absent_dev, args):
     oracle.build()
     keys = keys_dev.cpu().numpy().view(np.uint64)
     absent = absent_dev.cpu().numpy().view(np.uint64)
-    return cpu_step(wl, keys, absent, cpu_threads(args), oracle, kind="port")
+    return cpu_step(wl, keys, absent, cpu_threads(args), oracle, kind="port", parity=True)
 
 
-def cpu_step(wl, keys, absent, threads, oracle, kind):
+def cpu_step(wl, keys, absent, threads, oracle, kind, parity=False):
+    """One full step on the oracle; with parity, also the hashes of its
+    filter after the inserts and the deletes and of its count arrays, taken
+    outside the timed spans."""
     o = oracle.Oracle(wl.nbits, threads=threads)
+    par = {}
     t0 = time.perf_counter()
     for s, n in wl.batches:
         o.bulk_insert(keys[s:s + n])
     t1 = time.perf_counter()
+    if parity:
+        par["dump_insert"] = sha256_of(o.dump())
+    t1b = time.perf_counter()
     c1 = o.bulk_get(keys[: wl.n_get])
     c2 = o.bulk_get(absent)
     t2 = time.perf_counter()
     for s in range(0, wl.n_get, wl.batch):
         o.bulk_delete(keys[s:min(wl.n_get, s + wl.batch)])
     t3 = time.perf_counter()
+    if parity:
+        par["counts_present"] = sha256_of(c1.view(np.int64))
+        par["counts_absent"] = sha256_of(c2.view(np.int64))
+        par["false_positives"] = int((c2 > 0).sum())
+        par["dump_delete"] = sha256_of(o.dump())
     o.close()
-    dt = t3 - t0
+    t_ins, t_get, t_del = t1 - t0, t2 - t1b, t3 - t2
+    dt = t_ins + t_get + t_del
     assert (c1 > 0).all()
-    return {
+    res = {
         "value": round(wl.key_ops / dt / 1e6, 3),
         "unit": UNIT,
         "cores": threads,
@@ -1049,10 +1114,13 @@ def cpu_step(wl, keys, absent, threads, oracle, kind):
         "sample": f"the full step once ({wl.key_ops} key ops), {threads} threads: regions of one parity "
                   f"in parallel, as the reference's even/odd launch; hash + sort single-threaded",
         "seconds": round(dt, 3),
-        "ops": {"insert_mkeys_s": round(wl.n_insert / (t1 - t0) / 1e6, 3),
-                "get_mkeys_s": round(2 * wl.n_get / (t2 - t1) / 1e6, 3),
-                "delete_mkeys_s": round(wl.n_get / (t3 - t2) / 1e6, 3)},
+        "ops": {"insert_mkeys_s": round(wl.n_insert / t_ins / 1e6, 3),
+                "get_mkeys_s": round(2 * wl.n_get / t_get / 1e6, 3),
+                "delete_mkeys_s": round(wl.n_get / t_del / 1e6, 3)},
     }
+    if parity:
+        res["parity"] = par
+    return res
 
 
 def run_reference(args, wl, rank, world):

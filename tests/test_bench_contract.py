@@ -34,3 +34,33 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_parity_block_of_the_oracle_step():
+    """The parity block bench.py adds to its line: two sides that ran the same
+    step agree on every hash; a side whose filter differs by one byte is
+    reported unequal for that item only."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+
+    oracle.build()
+    wl = bench.Workload(14, 12, 12)
+    keys = oracle.splitmix64(1, wl.n_insert)
+    absent = oracle.splitmix64(2, wl.n_get)
+    a = bench.cpu_step(wl, keys, absent, 2, oracle, "port", parity=True)["parity"]
+    b = bench.cpu_step(wl, keys, absent, 1, oracle, "port", parity=True)["parity"]
+    assert set(bench.PARITY_KEYS) <= set(a)
+    p = bench.parity_block(14, {"oracle": a, "again": b, "absent": None})
+    assert p["compared"] == ["again", "oracle"]
+    assert p["dump_insert_equal"] and p["counts_present_equal"] and p["fp_set_equal"] and p["dump_delete_equal"]
+    o = oracle.Oracle(14)
+    o.bulk_insert(keys)
+    d = o.dump()
+    d[-1] ^= 1
+    c = dict(b, dump_insert=bench.sha256_of(d))
+    p = bench.parity_block(14, {"oracle": a, "changed": c})
+    assert not p["dump_insert_equal"] and p["dump_delete_equal"] and p["fp_set_equal"]
+    assert bench.sha256_of(np.arange(4, dtype=np.uint64)) == bench.sha256_of(np.arange(4, dtype=np.int64))

@@ -68,3 +68,52 @@ def test_reference_cuda_reduce_matches_oracle_and_product(refgpu, nbits):
         qf.bulk_insert_reduce(dev(keys))
         c = qf.export()
         assert np.array_equal(a, c), first_diff(a, c)
+
+
+@pytest.mark.slow
+def test_product_matches_reference_cuda_build_at_2_26_slots_90_percent(refgpu):
+    """The headline workload's shape at 2^26 slots: 90% of the slots filled in
+    2^22-key bulk_insert batches (256 keys per 4096-quotient region, as at
+    2^28 slots with 2^24-key batches), then 2^24 present and 2^24 absent gets
+    and 2^24 deletes.  The product's packed filter after the inserts and after
+    the deletes, and both count arrays (the false-positive set on the absent
+    keys), equal the reference's CUDA build word for word.  At this load the
+    short-window rebuild hands regions to the full-window pass, which is
+    checked to have run."""
+    import torch
+
+    import cqf_gb300
+    from cqf_gb300 import build, synth
+
+    build.build()
+    nbits, batch, nget = 26, 1 << 22, 1 << 24
+    n = int(0.9 * (1 << nbits))
+    keys = synth.splitmix64_dev(1, n)
+    absent = synth.splitmix64_dev(2, nget)
+    r = refgpu.RefGPU(nbits)
+    try:
+        with cqf_gb300.QF(nbits) as qf:
+            scratch = torch.empty(batch, dtype=torch.int64, device="cuda")
+            for s in range(0, n, batch):
+                m = min(batch, n - s)
+                qf.bulk_insert(keys[s:s + m], n=m)
+                scratch[:m].copy_(keys[s:s + m])
+                r.bulk_insert(scratch, m)  # overwrites its input with hashes
+            a, b = qf.export(), r.dump()
+            assert np.array_equal(a, b), first_diff(a, b)
+            assert qf.counters()["full_window_regions"] > 0
+            for probe in (keys[:nget], absent):
+                o1, o2 = zeros_dev(nget), zeros_dev(nget)
+                qf.bulk_get(probe, o1)
+                r.bulk_get(probe, o2)
+                torch.cuda.synchronize()
+                assert torch.equal(o1, o2)
+            for s in range(0, nget, batch):
+                qf.bulk_delete(keys[s:s + batch], n=batch)
+                scratch.copy_(keys[s:s + batch])
+                r.bulk_delete(scratch, batch)
+            a, b = qf.export(), r.dump()
+            assert np.array_equal(a, b), first_diff(a, b)
+            assert qf.status() & ~cqf_gb300.STATUS_DEFERRED == 0
+    finally:
+        r.close()
