@@ -77,7 +77,9 @@ struct Lay {
   static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8]
   static constexpr int OFF_KC = OFF_DELTA;                       // u32[KCW]
   static constexpr int OFF_RPOS = OFF_DELTA;                     // u16[WIN + 8]
-  static constexpr int OFF_NOCC = (OFF_DELTA + (WIN + 8) * 2 + 7) & ~7;  // u64[WB] new occupieds
+  // the single-round kernel keeps two u16 per key in the same table
+  static constexpr int DELTA_BYTES = (WIN + 8) * 2 > 4 * KMAX ? (WIN + 8) * 2 : 4 * KMAX;
+  static constexpr int OFF_NOCC = (OFF_DELTA + DELTA_BYTES + 7) & ~7;  // u64[WB] new occupieds
   static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
   static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
   static constexpr int OFF_RRANK = OFF_ORANK + (WB + 8) * 2;     // u16[WB + 8]
@@ -201,7 +203,10 @@ __device__ int merge_run(Img cur, bool has_old, int s, int e, const uint32_t* ke
   return total;
 }
 
-// Block-wide exclusive scan of max-plus maps f(x) = max(a, x + b).
+// Block-wide exclusive scan of max-plus maps f(x) = max(a, x + b).  Both
+// parts saturate at kNeg ("minus infinity"), so maps that reset their
+// argument (b = kNeg) compose without overflow.
+__device__ __forceinline__ int sat(int v) { return max(v, kNeg); }
 template <int NT>
 __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -210,8 +215,8 @@ __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
     int pa = __shfl_up_sync(0xffffffffu, ia, o);
     int pb = __shfl_up_sync(0xffffffffu, ib, o);
     if (lane >= o) {  // (pa,pb) first, then (ia,ib)
-      ia = max(ia, pa + ib);
-      ib = pb + ib;
+      ia = max(ia, sat(pa + ib));
+      ib = sat(pb + ib);
     }
   }
   if (lane == 31) { sa[wid] = ia; sb[wid] = ib; }
@@ -221,7 +226,7 @@ __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
     for (int o = 1; o < 32; o <<= 1) {
       int pa = __shfl_up_sync(0xffffffffu, wa, o);
       int pb = __shfl_up_sync(0xffffffffu, wb, o);
-      if (lane >= o) { wa = max(wa, pa + wb); wb = pb + wb; }
+      if (lane >= o) { wa = max(wa, sat(pa + wb)); wb = sat(pb + wb); }
     }
     sa[lane] = wa;
     sb[lane] = wb;
@@ -231,8 +236,8 @@ __device__ void scan_maps(int& a, int& b, int* sa, int* sb) {
   if (lane == 0) { ea = kNeg; eb = 0; }
   if (wid > 0) {
     int pa = sa[wid - 1], pb = sb[wid - 1];
-    ea = max(ea, pa + eb);
-    eb = pb + eb;
+    ea = max(ea, sat(pa + eb));
+    eb = sat(pb + eb);
   }
   a = ea;
   b = eb;
@@ -647,6 +652,436 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
   return true;
 }
 
+// The last word w of [0, nw) whose exclusive rank rank[w] is <= k: the word
+// holding the k-th set bit, when k is below the total.
+__device__ __forceinline__ int rank_word(const uint16_t* rank, int nw, int k) {
+  int lo = 0, hi = nw;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if ((int)rank[mid] <= k) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Single-round insert into region R (all threads of the CTA) in a window of
+// SPAN slots, by shifting slots instead of re-placing every run.
+//
+// The batch changes only the runs of its quotients (the touched runs: their
+// counters merged with the keys, merge_run) and adds runs for quotients that
+// had none.  Everything else keeps its bytes and moves right by a shift D(x)
+// that a recurrence over the old slots gives, one map per slot:
+//   D <- max(0, D + ins(x) - empty(x))
+// (growth ins(x) enters before slot x; an empty slot absorbs one slot of
+// push).  Each map has the form max(a, D + b), so one block-wide max-plus
+// scan gives every thread the shift at its first slot.  This is the
+// canonical layout's rule end(q) = max(q + L_q - 1, end(prev) + L_q) written
+// per slot: a touched run of old length l and new length L adds L - l before
+// the slot X after its end, a new run of quotient q adds L before slot
+// X = max(q, end of the runs before it + 1), and a run's new bytes go where
+// its old first slot moves.
+//
+// Threads own SPAN / 256 consecutive slots; the per-quotient work is per
+// touched run only (about one per thread), which finds its run from its
+// block's exact offset.  Returns false, having written nothing, when the
+// changes would reach past the window.  Deletes, and regions of more than
+// KMAX keys, go to rebuild_window.
+template <int LOGS, bool CNT, int SPAN, class Loc>
+__device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p, const uint32_t R) {
+  using L = Lay<LOGS, CNT>;
+  constexpr int NT = L::NT, WB = L::WB, REG = L::REG, KMAX = L::KMAX;
+  constexpr int qpt = SPAN / NT;  // slots per thread
+  constexpr int kFar = 1 << 20;   // a position past every window
+  static_assert(SPAN % NT == 0 && SPAN <= L::WIN, "slots split evenly over threads");
+  static_assert(4 * KMAX <= L::DELTA_BYTES, "per-key tables fit the shared table");
+  extern __shared__ __align__(128) uint8_t sm[];
+  __shared__ int s_i[8];
+  __shared__ int sa[32], sb[32];
+
+  const uint32_t kbeg = p.region_start[R];
+  const int nk = (int)p.region_count[R];
+  if (nk == 0) return true;
+  Geom g;
+  uint32_t r;
+  const quotient_filter* dq;
+  if (!loc.locate(R, LOGS, &g, &r, &dq)) return true;
+  const int tid = threadIdx.x;
+
+  const uint64_t base = (uint64_t)r << LOGS;
+  const uint64_t bw0 = base >> 6;
+  const int wb = (int)min((uint64_t)(SPAN / 64), g.nblocks - bw0);
+  const int wslots = wb * 64;
+  const int win_valid = (int)min((uint64_t)wslots, g.xnslots - base);
+  const int win_q = (int)min((uint64_t)SPAN, g.nslots - base);
+  const int wq_words = (win_q + 63) >> 6;
+
+  const Img C{sm + L::OFF_IMG0};
+  const Img N{sm + L::OFF_IMG1};
+  uint32_t* kg = reinterpret_cast<uint32_t*>(sm + L::OFF_KG);
+  uint32_t* kc = reinterpret_cast<uint32_t*>(sm + L::OFF_KC);
+  // growth entering before each slot, then the shift just before it
+  int16_t* ins = reinterpret_cast<int16_t*>(sm + L::OFF_PREF);
+  uint32_t* ins32 = reinterpret_cast<uint32_t*>(sm + L::OFF_PREF);
+  // after the grouping: each key's event slot X (its group's) and each
+  // group's old run length
+  uint16_t* gx = reinterpret_cast<uint16_t*>(sm + L::OFF_DELTA);
+  uint16_t* gl = reinterpret_cast<uint16_t*>(sm + L::OFF_DELTA + 2 * KMAX);
+  unsigned long long* nocc = reinterpret_cast<unsigned long long*>(sm + L::OFF_NOCC);
+  unsigned long long* trm = reinterpret_cast<unsigned long long*>(sm + L::OFF_TCH);  // touched runs' slots
+  uint16_t* orank = reinterpret_cast<uint16_t*>(sm + L::OFF_ORANK);
+  uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
+  uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
+
+  // ---- stage the window (wb blocks of 96 bytes) into image C
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(g.blocks + bw0);
+    uint4* dst = reinterpret_cast<uint4*>(C.p);
+    for (int i = tid; i < wb * 6; i += NT) dst[i] = src[i];
+  }
+  for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
+  for (int i = tid; i < (wslots >> 1); i += NT) ins32[i] = 0;
+  __syncthreads();
+  const int c0 = (int)C.off(0) - 1;  // last slot used by earlier regions' runs
+  if (c0 + 1 >= win_valid) return false;  // every run of this region lies past the window
+
+  auto runs_after_c0 = [&](int w) -> unsigned long long {
+    unsigned long long rw = C.run(w);
+    const int lo = 64 * w;
+    if (c0 >= lo + 63) return 0ULL;
+    if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
+    return rw;
+  };
+
+  // ---- group the keys by quotient (counting sort in shared memory)
+  for (int i = tid; i < nk; i += NT) {
+    const uint32_t q = p.keys[kbeg + i] >> 8;
+    atomicAdd(&kc[q >> 1], 1u << ((q & 1) * 16));
+  }
+  __syncthreads();
+  {
+    constexpr int WPT = (REG / 2) / NT;
+    const int a = tid * WPT;
+    int sum = 0;
+    for (int w = a; w < a + WPT; w++) sum += (int)(kc[w] & 0xFFFFu) + (int)(kc[w] >> 16);
+    int tot;
+    int run = scan_sum<NT>(sum, sa, &tot);
+    for (int w = a; w < a + WPT; w++) {
+      const uint32_t v = kc[w];
+      const uint32_t lo = (uint32_t)run;
+      run += (int)(v & 0xFFFFu);
+      const uint32_t hi = (uint32_t)run;
+      run += (int)(v >> 16);
+      kc[w] = lo | (hi << 16);
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < nk; i += NT) {
+    const uint32_t key = p.keys[kbeg + i];
+    const uint32_t q = key >> 8;
+    const uint32_t sh = (q & 1) * 16;
+    const uint32_t old = atomicAdd(&kc[q >> 1], 1u << sh);
+    kg[(old >> sh) & 0xFFFFu] = key;
+    if (CNT) kn[(old >> sh) & 0xFFFFu] = p.counts[kbeg + i];
+  }
+  // ---- rank tables of the old image: per window word, the occupied
+  // quotients and the runends after c0 before it
+  {
+    int packed = 0;
+    if (tid < WB) {
+      const int co = tid < wq_words ? __popcll(C.occ(tid)) : 0;
+      const int cr = tid < wb ? __popcll(runs_after_c0(tid)) : 0;
+      packed = co | (cr << 16);
+    }
+    int tot;
+    const int ex = scan_sum<NT>(packed, sa, &tot);  // synchronises: the grouping is done
+    if (tid < WB) {
+      orank[tid] = (uint16_t)(ex & 0xFFFF);
+      rrank[tid] = (uint16_t)(ex >> 16);
+      nocc[tid] = tid < wq_words ? C.occ(tid) : 0ULL;
+      trm[tid] = 0ULL;
+    }
+    if (tid == 0) s_i[1] = tot & 0xFFFF;
+  }
+  __syncthreads();
+  const int nold = s_i[1];  // occupied quotients of the window
+  auto rank_of = [&](int q) -> int {
+    return (int)orank[q >> 6] + __popcll(C.occ(q >> 6) & ((1ULL << (q & 63)) - 1ULL));
+  };
+  // the n-th (0-based) runend at or after slot `from` (> c0), or kFar
+  auto nth_end = [&](int from, int n) -> int {
+    int w = from >> 6;
+    if (w >= wb) return kFar;
+    unsigned long long m = C.run(w) & (~0ULL << (from & 63));
+    int c = __popcll(m);
+    while (n >= c) {
+      n -= c;
+      if (++w >= wb) return kFar;
+      m = C.run(w);
+      c = __popcll(m);
+    }
+    return 64 * w + select64(m, n);
+  };
+  auto group_end = [&](int ks, uint32_t q) -> int {
+    int ke = ks + 1;
+    while (ke < nk && (kg[ke] >> 8) == q) ke++;
+    return ke;
+  };
+
+  // ---- pass 1 over the touched quotients: the run each key group changes,
+  // its new length, and the growth it adds before slot X
+  bool my_defer = false;
+  for (int i = tid; i < nk; i += NT) {
+    const uint32_t q = kg[i] >> 8;
+    if (i > 0 && (kg[i - 1] >> 8) == q) continue;
+    const int ke = group_end(i, q);
+    for (int a = i + 1; a < ke; a++) {  // the quotient's keys by remainder
+      const uint32_t v = kg[a];
+      const uint32_t vc = CNT ? kn[a] : 0u;
+      int b = a;
+      while (b > i && kg[b - 1] > v) {
+        kg[b] = kg[b - 1];
+        if (CNT) kn[b] = kn[b - 1];
+        b--;
+      }
+      kg[b] = v;
+      if (CNT) kn[b] = vc;
+    }
+    // the runs of block qb's quotients end at the runends from its offset on
+    const int qb = (int)(q >> 6);
+    const unsigned long long ow = C.occ(qb);
+    const bool occ = (ow >> (q & 63)) & 1ULL;
+    const int rib = __popcll(ow & ((1ULL << (q & 63)) - 1ULL));
+    const int p0 = 64 * qb + (int)C.off(qb);
+    const int prev_end = rib ? nth_end(p0, rib - 1) : p0 - 1;
+    int s, e, X;
+    if (occ) {
+      e = prev_end >= kFar ? kFar : nth_end(prev_end + 1, 0);
+      s = max((int)q, prev_end + 1);
+      X = e + 1;
+    } else {
+      X = max((int)q, prev_end + 1);
+      s = X;
+      e = X - 1;
+    }
+    if (X >= win_valid) { my_defer = true; continue; }
+    const int len = merge_run<false, false>(C, occ, s, e, kg, kn, i, ke, N, 0);
+    const int delta = len - (e - s + 1);
+    if (delta < 0) { my_defer = true; continue; }  // counters never shrink on insert
+    if (delta) atomicAdd(&ins32[X >> 1], (uint32_t)delta << ((X & 1) * 16));
+    for (int a = i; a < ke; a++) gx[a] = (uint16_t)X;
+    gl[i] = (uint16_t)(e - s + 1);
+    if (occ) {
+      for (int w = s >> 6; w <= (e >> 6); w++) {
+        const int lo = max(s, 64 * w) - 64 * w, hi = min(e, 64 * w + 63) - 64 * w;
+        atomicOr(&trm[w], (~0ULL >> (63 - hi)) & (~0ULL << lo));
+      }
+    } else {
+      atomicOr(&nocc[q >> 6], 1ULL << (q & 63));
+    }
+  }
+  if (__syncthreads_or(my_defer)) return false;
+
+  // ---- the shift recurrence over this thread's slots [lo, hi): those after
+  // c0 and inside the window (the others neither move nor shift).  The map
+  // of slot x is max(a, D + b).
+  const int ca = tid * qpt;
+  const int lo = max(ca, c0 + 1), hi = min(ca + qpt, win_valid);
+  struct Walk {  // per-slot flags, advanced slot by slot from the rank tables
+    int w, o, k;
+    unsigned long long m, ow, tw;
+    bool prev_end, prev_tr;
+  };
+  auto walk_init = [&](Walk& W) {
+    W.w = lo >> 6;
+    W.m = runs_after_c0(W.w);
+    W.ow = W.w < wq_words ? C.occ(W.w) : 0ULL;
+    W.tw = trm[W.w];
+    W.k = (int)rrank[W.w] + __popcll(W.m & ((1ULL << (lo & 63)) - 1ULL));
+    W.o = lo < win_q ? rank_of(lo) : nold;  // occupied window quotients below lo
+    if (lo == c0 + 1) {
+      W.prev_end = false;
+      W.prev_tr = false;
+    } else {
+      const int y = lo - 1;
+      W.prev_end = (runs_after_c0(y >> 6) >> (y & 63)) & 1ULL;
+      W.prev_tr = (trm[y >> 6] >> (y & 63)) & 1ULL;
+    }
+  };
+  // Advances W over slot x (c0 < x < win_valid): whether it holds a run's
+  // slot, ends a run, belongs to a touched run, or receives growth (b: its
+  // map max(0, D + b)), and whether a touched run's writer needs the shift
+  // before it.
+  auto step = [&](Walk& W, int x, int& b, bool& used, bool& is_end, bool& tr, bool& evt) {
+    if ((x >> 6) != W.w) {
+      W.w = x >> 6;
+      W.m = runs_after_c0(W.w);
+      W.ow = W.w < wq_words ? C.occ(W.w) : 0ULL;
+      W.tw = trm[W.w];
+    }
+    const int bit = x & 63;
+    W.o += (int)((W.ow >> bit) & 1ULL);
+    is_end = (W.m >> bit) & 1ULL;
+    tr = (W.tw >> bit) & 1ULL;
+    const int gv = (int)ins[x];
+    evt = gv != 0 || (W.prev_tr && W.prev_end);
+    used = W.o > W.k;
+    b = gv - (used ? 0 : 1);
+    W.k += (int)is_end;
+    W.prev_end = is_end;
+    W.prev_tr = tr;
+  };
+  int fa = 0, fb = 0;  // composed map of this thread's slots (b >= -1: nothing saturates)
+  if (lo < hi) {
+    Walk W;
+    walk_init(W);
+    for (int x = lo; x < hi; x++) {
+      int b;
+      bool used, is_end, tr, evt;
+      step(W, x, b, used, is_end, tr, evt);
+      fa = max(0, fa + b);
+      fb += b;
+    }
+  }
+  int ea = fa, eb = fb;
+  scan_maps<NT>(ea, eb, sa, sb);
+  const int d_in = max(ea, eb);  // the shift entering this thread's slots (D = 0 before the window)
+  if (tid == NT - 1) s_i[2] = max(fa, sat(d_in + fb));  // the shift after the window's last slot
+  // ---- clear the new image; keep the previous region's spill
+  {
+    uint4* dst = reinterpret_cast<uint4*>(N.p);
+    for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
+  }
+  __syncthreads();
+  if (s_i[2] != 0) return false;  // the changes reach past the window
+  for (int sl = tid; sl <= c0 && sl < wslots; sl += NT) N.slot(sl) = C.slot(sl);
+  for (int w = tid; w < wb && 64 * w <= c0; w += NT) {
+    const int nb = c0 - 64 * w;  // bits 0..nb belong to the previous region's runs
+    N.run(w) = nb >= 63 ? C.run(w) : (C.run(w) & ((2ULL << nb) - 1ULL));
+  }
+  __syncthreads();
+  // ---- pass 2 over the slots: untouched slots move by their shift; the
+  // shift before each event slot is kept for the touched runs' writers
+  if (lo < hi) {
+    Walk W;
+    walk_init(W);
+    int D = d_in;
+    unsigned long long ebits = 0;
+    int ew = -1;
+    for (int x = lo; x < hi; x++) {
+      int b;
+      bool used, is_end, tr, evt;
+      step(W, x, b, used, is_end, tr, evt);
+      const int dp = D;
+      D = max(0, D + b);
+      if (evt) ins[x] = (int16_t)dp;
+      if (used && !tr) {
+        const int t = x + D;
+        N.slot(t) = C.slot(x);
+        if (is_end) {
+          if ((t >> 6) != ew) {
+            if (ebits) atomicOr(&N.run(ew), ebits);
+            ew = t >> 6;
+            ebits = 0;
+          }
+          ebits |= 1ULL << (t & 63);
+        }
+      }
+    }
+    if (ebits) atomicOr(&N.run(ew), ebits);
+  }
+  __syncthreads();
+  // ---- pass 2 over the touched quotients: each run's new bytes where its
+  // old first slot moved.  Runs whose growth enters before the same slot X
+  // (a touched run and the new runs right after it) are written in quotient
+  // order by the first of them.
+  for (int i = tid; i < nk; i += NT) {
+    const uint32_t q = kg[i] >> 8;
+    if (i > 0 && (kg[i - 1] >> 8) == q) continue;
+    const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
+    const int X = (int)gx[i];
+    if (i > 0 && (int)gx[i - 1] == X) continue;  // written by the first run of its slot
+    const int ell = (int)gl[i];
+    int ke = group_end(i, q);
+    int pos = X - ell + (int)ins[X];
+    int len = merge_run<false, true>(C, occ, X - ell, X - 1, kg, kn, i, ke, N, pos);
+    if (len > 0) atomicOr(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
+    pos += len;
+    while (ke < nk && (int)gx[ke] == X) {  // new runs entering before the same slot
+      const int ks = ke;
+      ke = group_end(ks, kg[ks] >> 8);
+      len = merge_run<false, true>(C, false, 0, -1, kg, kn, ks, ke, N, pos);
+      if (len > 0) atomicOr(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
+      pos += len;
+    }
+  }
+  __syncthreads();
+  // ---- block headers: occupieds, then offsets from the new run ends
+  {
+    int packed = 0;
+    if (tid < WB) {
+      const unsigned long long nw = tid < wq_words ? nocc[tid] : 0ULL;
+      unsigned long long rw = 0ULL;
+      if (tid < wb) {
+        N.occ(tid) = nw;
+        rw = N.run(tid);
+        const int l0 = 64 * tid;
+        if (c0 >= l0 + 63) rw = 0ULL;
+        else if (c0 >= l0) rw &= ~0ULL << (c0 - l0 + 1);
+      }
+      packed = __popcll(nw) | (__popcll(rw) << 16);
+    }
+    int tot;
+    const int ex = scan_sum<NT>(packed, sa, &tot);
+    if (tid < WB) {
+      orank[tid] = (uint16_t)(ex & 0xFFFF);  // now: new occupied quotients before word tid
+      rrank[tid] = (uint16_t)(ex >> 16);     // new runends after c0 before word tid
+    }
+    if (tid == 0) s_i[3] = tot >> 16;
+  }
+  __syncthreads();
+  {
+    const int nvis_new = s_i[3];
+    for (int w = tid; w < wb; w += NT) {
+      if (w == 0) {
+        N.off(0) = C.off(0);
+        continue;
+      }
+      const int kq = (int)orank[w];  // new runs of quotients before block w
+      int E;
+      if (kq == 0) {
+        E = c0;
+      } else if (kq - 1 < nvis_new) {
+        const int ww = rank_word(rrank, wb, kq - 1);
+        unsigned long long rw = N.run(ww);
+        const int l0 = 64 * ww;
+        if (c0 >= l0 + 63) rw = 0ULL;
+        else if (c0 >= l0) rw &= ~0ULL << (c0 - l0 + 1);
+        E = 64 * ww + select64(rw, kq - 1 - (int)rrank[ww]);
+      } else {
+        E = win_valid;  // ends past the window: unchanged
+      }
+      N.off(w) = E >= win_valid ? C.off(w) : (uint32_t)max(0, E - 64 * w + 1);
+    }
+  }
+  __syncthreads();
+  // ---- write back the blocks that differ from what was loaded
+  {
+    const uint4* fin = reinterpret_cast<const uint4*>(N.p);
+    const uint4* org = reinterpret_cast<const uint4*>(C.p);
+    uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0);
+    for (int w = tid; w < wb; w += NT) {
+      bool diff = false;
+      for (int c = 0; c < 6; c++) {
+        const uint4 a = fin[w * 6 + c], b = org[w * 6 + c];
+        diff |= (a.x != b.x) | (a.y != b.y) | (a.z != b.z) | (a.w != b.w);
+      }
+      if (diff)
+        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
+    }
+  }
+  return true;
+}
+
 // Where a rebuild launch finds its regions: one CTA per region of the
 // parity, in region order; or a persistent grid whose CTAs take regions
 // one at a time from a work list (k_sparse's, or the short pass's retries)
@@ -663,9 +1098,16 @@ __global__ void __launch_bounds__(256, CNT ? 3 : Cfg<LOGS>::MINB) k_rebuild(Loc 
   using L = Lay<LOGS, CNT>;
   constexpr bool kShort = SPAN < L::WIN;
   auto one = [&](uint32_t R) {
-    const bool ok = (kShort && p.region_count[R] > (uint32_t)L::KMAX)
-                        ? false
-                        : rebuild_window<LOGS, DEL, CNT, SPAN>(loc, p, R);
+    // inserts of one round of keys shift the window; deletes, and keys
+    // needing several rounds (full window only), re-place every run
+    bool ok;
+    if constexpr (!DEL) {
+      if (p.region_count[R] <= (uint32_t)L::KMAX) ok = shift_window<LOGS, CNT, SPAN>(loc, p, R);
+      else ok = kShort ? false : rebuild_window<LOGS, DEL, CNT, SPAN>(loc, p, R);
+    } else {
+      ok = (kShort && p.region_count[R] > (uint32_t)L::KMAX) ? false
+                                                             : rebuild_window<LOGS, DEL, CNT, SPAN>(loc, p, R);
+    }
     if (ok || threadIdx.x != 0) return;
     if (kShort) {
       const uint32_t at = atomicAdd(&p.retry[kListCount], 1u);
