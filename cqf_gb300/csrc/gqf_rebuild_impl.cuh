@@ -38,6 +38,18 @@ namespace {
 
 constexpr int kNeg = -(1 << 28);  // "minus infinity" of the max-plus scan
 
+// OR of a 64-bit mask into a shared-memory word as native 32-bit atomics on
+// the halves that carry bits.
+__device__ __forceinline__ void or64(unsigned long long* p, unsigned long long v) {
+  uint32_t* h = reinterpret_cast<uint32_t*>(p);
+  if ((uint32_t)v) atomicOr(h, (uint32_t)v);
+  if ((uint32_t)(v >> 32)) atomicOr(h + 1, (uint32_t)(v >> 32));
+}
+// Sets bit i of a shared-memory bitmap of 64-bit words.
+__device__ __forceinline__ void set_bit(unsigned long long* m, int i) {
+  atomicOr(reinterpret_cast<uint32_t*>(m) + (i >> 5), 1u << (i & 31));
+}
+
 template <int LOGS>
 struct Cfg;
 // PUSH: the slots past the region a window holds; TAIL: the shorter tail
@@ -439,7 +451,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
       const uint32_t q = kg[i] >> 8;
       if (i > 0 && (kg[i - 1] >> 8) == q) continue;
       const int ks = i, ke = group_end(i, q);
-      atomicOr(&tch[q >> 6], 1ULL << (q & 63));
+      set_bit(tch, (int)q);
       const bool occ = (C.occ(q >> 6) >> (q & 63)) & 1ULL;
       int s = 0, e = -1;
       if (occ) {
@@ -528,7 +540,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
       int nd = delta[k];                   // the next run's old start, loaded ahead
       for (int q = ca; q < qb_; q++) {
         if ((q >> 6) != cw) {
-          if (cw >= 0 && occ_bits) atomicOr(&nocc[occ_word], occ_bits);
+          if (cw >= 0 && occ_bits) or64(&nocc[occ_word], occ_bits);
           occ_bits = 0;
           cw = occ_word = q >> 6;
           ow = C.occ(cw);
@@ -542,7 +554,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
           occ_bits |= 1ULL << (q & 63);
           if (x < wslots) {
             if ((x >> 6) != ew) {
-              if (ebits) atomicOr(&N.run(ew), ebits);
+              if (ebits) or64(&N.run(ew), ebits);
               ew = x >> 6;
               ebits = 0;
             }
@@ -556,8 +568,8 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
         }
         pref[q] = (uint16_t)(x + 1);
       }
-      if (occ_bits) atomicOr(&nocc[occ_word], occ_bits);
-      if (ebits) atomicOr(&N.run(ew), ebits);
+      if (occ_bits) or64(&nocc[occ_word], occ_bits);
+      if (ebits) or64(&N.run(ew), ebits);
     }
     __syncthreads();
     {
@@ -873,10 +885,10 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
     if (occ) {
       for (int w = s >> 6; w <= (e >> 6); w++) {
         const int lo = max(s, 64 * w) - 64 * w, hi = min(e, 64 * w + 63) - 64 * w;
-        atomicOr(&trm[w], (~0ULL >> (63 - hi)) & (~0ULL << lo));
+        or64(&trm[w], (~0ULL >> (63 - hi)) & (~0ULL << lo));
       }
     } else {
-      atomicOr(&nocc[q >> 6], 1ULL << (q & 63));
+      set_bit(nocc, (int)q);
     }
   }
   if (__syncthreads_or(my_defer)) return false;
@@ -979,7 +991,7 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
         N.slot(t) = C.slot(x);
         if (is_end) {
           if ((t >> 6) != ew) {
-            if (ebits) atomicOr(&N.run(ew), ebits);
+            if (ebits) or64(&N.run(ew), ebits);
             ew = t >> 6;
             ebits = 0;
           }
@@ -987,7 +999,7 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
         }
       }
     }
-    if (ebits) atomicOr(&N.run(ew), ebits);
+    if (ebits) or64(&N.run(ew), ebits);
   }
   __syncthreads();
   // ---- pass 2 over the touched quotients: each run's new bytes where its
@@ -1004,13 +1016,13 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
     int ke = group_end(i, q);
     int pos = X - ell + (int)ins[X];
     int len = merge_run<false, true>(C, occ, X - ell, X - 1, kg, kn, i, ke, N, pos);
-    if (len > 0) atomicOr(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
+    if (len > 0) or64(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
     pos += len;
     while (ke < nk && (int)gx[ke] == X) {  // new runs entering before the same slot
       const int ks = ke;
       ke = group_end(ks, kg[ks] >> 8);
       len = merge_run<false, true>(C, false, 0, -1, kg, kn, ks, ke, N, pos);
-      if (len > 0) atomicOr(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
+      if (len > 0) or64(&N.run((pos + len - 1) >> 6), 1ULL << ((pos + len - 1) & 63));
       pos += len;
     }
   }
