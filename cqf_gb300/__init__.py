@@ -64,6 +64,7 @@ SIGNATURES = {
     "gqf_multi_merge": (_int, [_vp, _int, _vp]),
     "gqf_intersect": (_int, [_vp, _vp, _vp]),
     "gqf_inner_product": (_u64, [_vp, _vp]),
+    "gqf_resize": (_int, [_vp, _int]),
     "gqf_set_create": (_int, [_u32, _vp, _u64, ctypes.POINTER(_vp)]),
     "gqf_set_destroy": (None, [_vp]),
     "gqf_set_insert": (_int, [_vp, _vp, _vp, _u64, _u8, _vp]),
@@ -352,6 +353,12 @@ class QF:
 
     def inner_product(self, other: "QF") -> int:
         return int(self.L.gqf_inner_product(self.h, other.h))
+
+    def resize(self, new_nbits: int):
+        """Grows the table to 2^new_nbits slots under the same handle, keeping
+        every stored key (modulo 2^(nbits + 8)) and its count."""
+        self._ok(self.L.gqf_resize(self.h, int(new_nbits)))
+        self.nbits = int(new_nbits)
 
     def export(self) -> np.ndarray:
         n = int(self.L.gqf_export_size(self.h))

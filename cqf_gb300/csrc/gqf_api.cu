@@ -312,6 +312,50 @@ extern "C" {
 const char* gqf_last_error(void) { return g_err.c_str(); }
 const char* gqf_version(void) { return "gqf_gb300 0.1 (sm_103a)"; }
 
+}  // extern "C"
+
+namespace {
+// Sizes the table of a 2^nbits-slot filter into h (qf_init, src/gqf.cu:
+// 1939-1996, for qf_malloc_device's parameters) and allocates its zeroed
+// blocks and locks; on failure nothing stays allocated.
+bool alloc_table(quotient_filter& h, int nbits) {
+  h.nslots = 1ULL << nbits;
+  // qf_init (src/gqf.cu:1950-1951): xnslots = nslots + 10 sqrt(nslots)
+  h.xnslots = h.nslots + (uint64_t)(10 * std::sqrt((double)h.nslots));
+  h.nblocks = (h.xnslots + 63) / 64;
+  h.range = h.nslots << 8;
+  h.nbits = (uint32_t)nbits;
+  h.key_bits = (uint32_t)nbits + 8;
+  h.nlocks = h.xnslots / kLockRegion + 2;  // num_locks, src/gqf.cu:1996
+  h.blocks = nullptr;
+  h.locks = nullptr;
+  const bool ok = ck(cudaMalloc((void**)&h.blocks, h.nblocks * sizeof(Block)), "cudaMalloc blocks") &&
+                  ck(cudaMemset(h.blocks, 0, h.nblocks * sizeof(Block)), "cudaMemset blocks") &&
+                  ck(cudaMalloc((void**)&h.locks, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMalloc locks") &&
+                  ck(cudaMemset(h.locks, 0, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMemset locks");
+  if (!ok) {
+    if (h.blocks) cudaFree(h.blocks);
+    if (h.locks) cudaFree(h.locks);
+    h.blocks = nullptr;
+    h.locks = nullptr;
+  }
+  return ok;
+}
+
+void set_geometry(HostFilter* f) {
+  const quotient_filter& h = f->h;
+  f->g.blocks = h.blocks;
+  f->g.nslots = h.nslots;
+  f->g.xnslots = h.xnslots;
+  f->g.nblocks = h.nblocks;
+  f->g.range = h.range;
+  f->g.mask = h.range - 1;
+  f->g.nbits = h.nbits;
+}
+}  // namespace
+
+extern "C" {
+
 void qf_malloc_device(QF** qf, int nbits, bool bulk_config) {
   (void)bulk_config;
   if (!qf) return;
@@ -322,20 +366,9 @@ void qf_malloc_device(QF** qf, int nbits, bool bulk_config) {
   }
   HostFilter* f = new HostFilter();
   quotient_filter& h = f->h;
-  h.nslots = 1ULL << nbits;
-  // qf_init (src/gqf.cu:1950-1951): xnslots = nslots + 10 sqrt(nslots)
-  h.xnslots = h.nslots + (uint64_t)(10 * std::sqrt((double)h.nslots));
-  h.nblocks = (h.xnslots + 63) / 64;
-  h.range = h.nslots << 8;
-  h.nbits = (uint32_t)nbits;
-  h.key_bits = (uint32_t)nbits + 8;
-  h.nlocks = h.xnslots / kLockRegion + 2;  // num_locks, src/gqf.cu:1996
   h.lock_spin_limit = 1u << 20;
   f->device = current_device();
-  bool ok = ck(cudaMalloc((void**)&h.blocks, h.nblocks * sizeof(Block)), "cudaMalloc blocks") &&
-            ck(cudaMemset(h.blocks, 0, h.nblocks * sizeof(Block)), "cudaMemset blocks") &&
-            ck(cudaMalloc((void**)&h.locks, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMalloc locks") &&
-            ck(cudaMemset(h.locks, 0, h.nlocks * kLockStride * sizeof(uint32_t)), "cudaMemset locks") &&
+  bool ok = alloc_table(h, nbits) &&
             ck(cudaMalloc((void**)&f->aux, 256), "cudaMalloc aux") &&
             ck(cudaMemset(f->aux, 0, 256), "cudaMemset aux");
   if (ok) {
@@ -351,13 +384,7 @@ void qf_malloc_device(QF** qf, int nbits, bool bulk_config) {
     delete f;
     return;
   }
-  f->g.blocks = h.blocks;
-  f->g.nslots = h.nslots;
-  f->g.xnslots = h.xnslots;
-  f->g.nblocks = h.nblocks;
-  f->g.range = h.range;
-  f->g.mask = h.range - 1;
-  f->g.nbits = h.nbits;
+  set_geometry(f);
   f->log_region = auto_log_region(nbits);
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -825,22 +852,26 @@ uint64_t enum_prepare(HostFilter* f, cudaStream_t st, uint32_t** start) {
   return total;
 }
 
-// Inserts (hash, count) pairs into f with the counted rebuild.
-int insert_pairs(HostFilter* f, const uint64_t* h, const uint32_t* c, uint64_t n, cudaStream_t st) {
+// Inserts (hash, count) pairs into f with the counted rebuild (or (key,
+// count) pairs, hashed for f, when key_is_hash is 0).
+int insert_pairs(HostFilter* f, const uint64_t* h, const uint32_t* c, uint64_t n, cudaStream_t st,
+                 int key_is_hash = 1) {
   std::lock_guard<std::mutex> lk(f->mu);
   if (n == 0) return 0;
   if (!ensure_partition(f, n, true, st)) return -1;
   Partition p = f->part;
-  if (!ck(launch_partition_counted(f->g, p, h, c, n, nullptr, 1, status_ptr(f), st), "partition") ||
+  if (!ck(launch_partition_counted(f->g, p, h, c, n, nullptr, key_is_hash, status_ptr(f), st), "partition") ||
       !ck(launch_merge_regions(p, st), "merge_regions") ||
       !ck(launch_rebuild(f->g, p, Op::kInsert, f->dqf, status_ptr(f), st, sparse_max_for(f, n)), "rebuild"))
     return -1;
   return 0;
 }
 
-// The pairs of several filters, concatenated, as hashes and uint32 counts in
-// one device allocation (freed by the caller); *n gets the total.
-bool collect_pairs(std::vector<HostFilter*> fs, cudaStream_t st, uint64_t** h, uint32_t** c, uint64_t* n) {
+// The pairs of several filters, concatenated, as hashes (or keys, with
+// as_keys) and uint32 counts in one device allocation (freed by the caller);
+// *n gets the total.
+bool collect_pairs(std::vector<HostFilter*> fs, cudaStream_t st, uint64_t** h, uint32_t** c, uint64_t* n,
+                   int as_keys = 0) {
   std::vector<uint32_t*> starts;
   std::vector<uint64_t> counts;
   uint64_t total = 0;
@@ -865,7 +896,8 @@ bool collect_pairs(std::vector<HostFilter*> fs, cudaStream_t st, uint64_t** h, u
            ck(cudaMallocAsync((void**)&flag, 4, st), "cudaMallocAsync") && ck(cudaMemsetAsync(flag, 0, 4, st), "memset");
   uint64_t at = 0;
   for (size_t i = 0; good && i < starts.size(); i++) {
-    good = ck(launch_enum_write(fs[i]->g, starts[i] + fs[i]->h.nblocks, 0, *h + at, nullptr, *c + at, flag, st),
+    good = ck(launch_enum_write(fs[i]->g, starts[i] + fs[i]->h.nblocks, as_keys, *h + at, nullptr, *c + at, flag,
+                                st),
               "enumerate");
     at += counts[i];
   }
@@ -946,6 +978,46 @@ int gqf_multi_merge(QF* const* in, int nin, QF* out) {
   cudaFreeAsync(h, st);
   cudaFreeAsync(c, st);
   return ck(cudaStreamSynchronize(st), "sync") ? rc : -1;
+}
+
+// Grows the table under the same handle: every stored key (the inverse hash
+// of each stored hash, the key modulo 2^(nbits + 8)) with its count goes
+// into a 2^new_nbits-slot table, hashed over new_nbits + 8 bits.
+int gqf_resize(QF* qf, int new_nbits) {
+  HostFilter* f = lookup(qf);
+  if (!f) return -1;
+  if (new_nbits < (int)f->h.nbits || new_nbits > 36) {
+    set_err("gqf_resize: new_nbits must lie in [nbits, 36]");
+    return -1;
+  }
+  if (new_nbits == (int)f->h.nbits) return 0;
+  if (!ck(cudaStreamSynchronize(f->stream), "sync")) return -1;
+  cudaStream_t st = 0;
+  uint64_t* keys = nullptr;
+  uint32_t* c = nullptr;
+  uint64_t n = 0;
+  if (!collect_pairs({f}, st, &keys, &c, &n, 1)) return -1;
+  bool ok = ck(cudaStreamSynchronize(st), "sync");
+  if (ok) {
+    std::lock_guard<std::mutex> lk(f->mu);
+    quotient_filter nh = f->h;
+    ok = alloc_table(nh, new_nbits);
+    if (ok) {
+      cudaFree(f->h.blocks);
+      cudaFree(f->h.locks);
+      if (f->packed) cudaFree(f->packed);
+      f->packed = nullptr;
+      f->h = nh;
+      set_geometry(f);
+      if (f->auto_region) f->log_region = auto_log_region(new_nbits);
+      ok = ck(cudaMemcpy(f->dqf, &f->h, sizeof(quotient_filter), cudaMemcpyHostToDevice), "cudaMemcpy descriptor");
+    }
+  }
+  int rc = ok ? insert_pairs(f, keys, c, n, st, 0) : -1;
+  cudaFreeAsync(keys, st);
+  cudaFreeAsync(c, st);
+  if (!ck(cudaStreamSynchronize(st), "sync")) rc = -1;
+  return rc;
 }
 
 int gqf_merge(QF* a, QF* b, QF* out) {

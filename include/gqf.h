@@ -223,6 +223,22 @@ int gqf_multi_merge(QF* const* in, int nin, QF* out);
 int gqf_intersect(QF* a, QF* b, QF* out);
 uint64_t gqf_inner_product(QF* a, QF* b);
 
+/* Resize: replaces qf_resize_malloc / qf_resize (src/gqf.cu:2301-2372, host
+ * filters only in the reference).  Grows the table to 2^new_nbits slots under
+ * the same QF handle and re-inserts every stored key with its count (counted
+ * rebuild); synchronises.  The reference keeps key_bits, so its resized
+ * filter stores narrower remainders (a 2^20-slot filter with 28 key bits
+ * resized to 2^21 slots keeps 7-bit remainders); this filter's slots are 8
+ * bits, so key_bits grows with the table (new_nbits + 8) and the false-
+ * positive rate stays that of a filter built at the new size.  Stored keys
+ * are recovered through the invertible hash, as qfi_get_key does, modulo
+ * 2^(nbits + 8): keys that fit those bits give exactly the filter built at
+ * the new size from the same multiset; wider keys keep their low bits (keys
+ * that collided stay merged).  new_nbits in [nbits, 36]; counters above
+ * 2^32 - 1 cannot be carried (-1).  On -1 after the old table was released,
+ * the filter is left empty at the new size. */
+int gqf_resize(QF* qf, int new_nbits);
+
 /* ------------------------------------------------------------- filter sets
  * No counterpart in the reference (one QF handle per filter, one bulk call
  * sequence per filter).  A set holds n independent filters (filter f has

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.gpu_util import dev, first_diff
+from tests.gpu_util import dev, first_diff, gpu_get
 
 pytestmark = pytest.mark.gpu
 
@@ -94,3 +94,51 @@ def test_intersect_and_inner_product(gq, na, nb):
         want = oracle.canonical_dump(out_bits, common)
         got = r.export()
         assert np.array_equal(got, want), first_diff(got, want)
+
+
+@pytest.mark.parametrize("old,new", [(12, 13), (16, 19), (20, 22)])
+def test_resize_equals_the_filter_built_at_the_new_size(gq, old, new):
+    """Keys that fit nbits + 8 bits (with repeats and one hot key): the
+    resized filter is word for word the oracle's filter built at the new size
+    from the same multiset, and the handle keeps working for gets and inserts."""
+    mask = np.uint64((1 << (old + 8)) - 1)
+    n = int(0.8 * (1 << old))
+    keys = np.concatenate([oracle.splitmix64(31, n) & mask, oracle.skewed_keys(32, n // 4, old - 4) & mask,
+                           np.full(300, 12345, dtype=np.uint64)])
+    qf = gq.QF(old)
+    try:
+        qf.bulk_insert(dev(keys))
+        qf.resize(new)
+        o = oracle.Oracle(new)
+        o.bulk_insert(keys)
+        a, b = qf.export(), o.dump()
+        assert np.array_equal(a, b), first_diff(a, b)
+        more = oracle.splitmix64(33, 1 << (new - 3)) & np.uint64((1 << (new + 8)) - 1)
+        qf.bulk_insert(dev(more))
+        o.bulk_insert(more)
+        assert np.array_equal(qf.export(), o.dump())
+        probe = np.concatenate([keys[:5000], oracle.splitmix64(34, 5000)])
+        assert np.array_equal(gpu_get(qf, probe), o.bulk_get(probe))
+        assert qf.status() & ~gq.STATUS_DEFERRED == 0
+    finally:
+        qf.close()
+
+
+def test_resize_keeps_the_low_bits_of_wider_keys(gq):
+    """Keys wider than nbits + 8 bits are stored by their low bits: after the
+    resize the filter equals one built at the new size from those low bits."""
+    old, new = 14, 16
+    keys = oracle.splitmix64(35, int(0.7 * (1 << old)))
+    low = keys & np.uint64((1 << (old + 8)) - 1)
+    qf = gq.QF(old)
+    try:
+        qf.bulk_insert(dev(keys))
+        qf.resize(new)
+        o = oracle.Oracle(new)
+        o.bulk_insert(low)
+        assert np.array_equal(qf.export(), o.dump())
+        with pytest.raises(RuntimeError):
+            qf.resize(new - 1)
+    finally:
+        qf.close()
+
