@@ -195,6 +195,38 @@ bool ensure_partition(HostFilter* f, uint64_t nkeys, bool with_counts, cudaStrea
     f->part.retry = base + 4ULL * cap;
     f->region_cap = cap;
   }
+  // staging of the two-level partition (large batches); without it those
+  // batches take the single-level path
+  if (const uint64_t words = stage_words(nkeys, nr, f->log_region)) {
+    Partition& p = f->part;
+    if (nkeys > p.stage_keys || (with_counts && !p.stage_counts)) {
+      const uint64_t cap = nkeys > p.stage_keys ? nkeys + nkeys / 8 + 1024 : p.stage_keys;
+      const bool had_counts = p.stage_counts != nullptr;
+      if (p.stage) cudaFreeAsync(p.stage, st);
+      if (p.stage_counts) cudaFreeAsync(p.stage_counts, st);
+      p.stage = p.stage_counts = nullptr;
+      p.stage_keys = 0;
+      if (cudaMallocAsync((void**)&p.stage, cap * sizeof(uint32_t), st) != cudaSuccess) {
+        p.stage = nullptr;
+      } else if ((with_counts || had_counts) &&
+                 cudaMallocAsync((void**)&p.stage_counts, cap * sizeof(uint32_t), st) != cudaSuccess) {
+        p.stage_counts = nullptr;
+        cudaFreeAsync(p.stage, st);
+        p.stage = nullptr;
+      } else {
+        p.stage_keys = cap;
+      }
+    }
+    if (words > p.tile_words) {
+      if (p.tiles) cudaFreeAsync(p.tiles, st);
+      p.tiles = nullptr;
+      p.tile_words = 0;
+      const uint64_t cap = words + words / 8 + 64;
+      if (cudaMallocAsync((void**)&p.tiles, cap * sizeof(uint32_t), st) == cudaSuccess) p.tile_words = cap;
+      else p.tiles = nullptr;
+    }
+    cudaGetLastError();  // a failed staging allocation is not an error: the single level runs
+  }
   f->part.nregions = nr;
   f->part.log_region = f->log_region;
   f->part.stats = stats_ptr(f);
@@ -410,6 +442,9 @@ void qf_destroy_device(QF* qf) {
   if (f->merge_h) cudaFree(f->merge_h);
   if (f->merge_c) cudaFree(f->merge_c);
   if (f->part.region_count) cudaFree(f->part.region_count);
+  if (f->part.stage) cudaFree(f->part.stage);
+  if (f->part.stage_counts) cudaFree(f->part.stage_counts);
+  if (f->part.tiles) cudaFree(f->part.tiles);
   if (f->packed) cudaFree(f->packed);
   cudaFree(f->h.blocks);
   cudaFree(f->h.locks);

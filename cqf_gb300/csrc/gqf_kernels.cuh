@@ -67,7 +67,18 @@ struct Partition {
                               // the full window (or nullptr)
   uint32_t nregions;
   int log_region;          // a region is 2^log_region quotients
+  // Staging of the two-level partition of large batches (launch_partition*),
+  // or nullptr for the single-level path: a packed entry per key, its count,
+  // and the per-tile bucket histograms (stage_words(...) words).
+  uint32_t* stage;
+  uint32_t* stage_counts;
+  uint32_t* tiles;
+  uint64_t stage_keys;     // entries stage holds
+  uint64_t tile_words;     // words tiles holds
 };
+// Words of Partition::tiles a batch of n keys needs (0: the single-level
+// path runs for such batches).
+uint64_t stage_words(uint64_t n, uint32_t nregions, int log_region);
 
 enum class Op : int { kInsert = 0, kDelete = 1 };
 

@@ -157,3 +157,32 @@ def test_kmer_shape_errors(gq):
     with gq.QF(10) as qf:
         with pytest.raises(RuntimeError):
             qf.bulk_insert_kmers(reads, 0)
+
+
+@pytest.mark.slow
+def test_two_level_partition_matches_oracle(gq):
+    """Batches of at least 2^18 keys into at least 4096 regions take the
+    two-level partition (tile histograms, staged scatter, one pass per
+    super-bucket).  Plain inserts with out-of-range pre-hashed keys mixed in,
+    a skewed counted batch with one hot key, and deletes: each equals the
+    oracle word for word, and the bad keys are skipped and flagged."""
+    nbits = 24
+    o = oracle.Oracle(nbits, threads=8)
+    with gq.QF(nbits) as qf:
+        h = oracle.hash64(oracle.splitmix64(41, 1 << 20), nbits)
+        bad = np.array([1 << (nbits + 8), (1 << 63) + 7, 1 << 40], dtype=np.uint64)
+        qf.bulk_insert(dev(np.concatenate([h[:1000], bad, h[1000:]])), flags=gq.QF_NO_LOCK | gq.QF_KEY_IS_HASH)
+        o.bulk_insert(h, key_is_hash=True)
+        assert qf.status() & gq.STATUS_BAD_KEY
+        assert np.array_equal(qf.export(), o.dump())
+        skew = np.concatenate([synth.zipf_keys(42, 1 << 21, 1 << 14), np.full(1 << 18, 777, dtype=np.uint64)])
+        qf.bulk_insert_reduce(dev(skew))
+        o.bulk_insert_reduce(skew)
+        a, b = o.dump(), qf.export()
+        assert np.array_equal(a, b), first_diff(a, b)
+        gone = oracle.hash64(oracle.splitmix64(41, 1 << 19), nbits)
+        qf.bulk_delete(dev(gone), flags=gq.QF_NO_LOCK | gq.QF_KEY_IS_HASH)
+        o.bulk_delete(gone, key_is_hash=True)
+        a, b = o.dump(), qf.export()
+        assert np.array_equal(a, b), first_diff(a, b)
+        assert qf.status() & gq.STATUS_FULL == 0
