@@ -50,6 +50,51 @@ __device__ __forceinline__ void set_bit(unsigned long long* m, int i) {
   atomicOr(reinterpret_cast<uint32_t*>(m) + (i >> 5), 1u << (i & 31));
 }
 
+// Bulk staging of a window: one thread starts a cp.async.bulk copy from
+// global into this CTA's shared memory that completes on an mbarrier, while
+// the other threads clear their tables; then all wait on the barrier's phase.
+// The wait is bounded (kStageSpin polls): a copy that never lands makes the
+// region fall back to the serial path and sets the timeout status bit.
+struct BulkStage {
+  unsigned long long* bar;  // mbarrier in shared memory, one arrival per phase
+  uint32_t phase;           // the phase the next copy completes
+  uint32_t* status;
+};
+constexpr uint32_t kStageSpin = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Thread 0: copies `bytes` (a multiple of 16, both addresses 16-byte
+// aligned) from src to dst and arms the barrier for them.
+__device__ __forceinline__ void bulk_stage_start(const BulkStage& sg, void* dst, const void* src, uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of dst come first
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(sg.bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(sg.bar))
+      : "memory");
+}
+
+// All threads: waits for the copy; false when the wait ran out.
+__device__ __forceinline__ bool bulk_stage_wait(BulkStage& sg) {
+  uint32_t done = 0;
+  for (uint32_t i = 0; i < kStageSpin && !done; i++) {
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_u32(sg.bar)), "r"(sg.phase)
+        : "memory");
+  }
+  sg.phase ^= 1u;
+  if (!done && threadIdx.x == 0) atomicOr(sg.status, kStTimeout);
+  return done != 0;
+}
+
 template <int LOGS>
 struct Cfg;
 // PUSH: the slots past the region a window holds; TAIL: the shorter tail
@@ -699,7 +744,7 @@ __device__ __forceinline__ int rank_word(const uint16_t* rank, int nw, int k) {
 // changes would reach past the window.  Deletes, and regions of more than
 // KMAX keys, go to rebuild_window.
 template <int LOGS, bool CNT, int SPAN, class Loc>
-__device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p, const uint32_t R) {
+__device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p, const uint32_t R, BulkStage& sg) {
   using L = Lay<LOGS, CNT>;
   constexpr int NT = L::NT, WB = L::WB, REG = L::REG, KMAX = L::KMAX;
   constexpr int qpt = SPAN / NT;  // slots per thread
@@ -744,15 +789,14 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
   uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
 
-  // ---- stage the window (wb blocks of 96 bytes) into image C
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(g.blocks + bw0);
-    uint4* dst = reinterpret_cast<uint4*>(C.p);
-    for (int i = tid; i < wb * 6; i += NT) dst[i] = src[i];
-  }
+  // ---- stage the window (wb blocks of 96 bytes) into image C with one
+  // bulk copy, clearing the tables meanwhile
+  if (tid == 0) bulk_stage_start(sg, C.p, g.blocks + bw0, (uint32_t)wb * 96u);
   for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
   for (int i = tid; i < (wslots >> 1); i += NT) ins32[i] = 0;
+  const bool staged = bulk_stage_wait(sg);
   __syncthreads();
+  if (!staged) return false;
   const int c0 = (int)C.off(0) - 1;  // last slot used by earlier regions' runs
   if (c0 + 1 >= win_valid) return false;  // every run of this region lies past the window
 
@@ -1109,12 +1153,18 @@ __global__ void __launch_bounds__(256, CNT ? 3 : Cfg<LOGS>::MINB) k_rebuild(Loc 
                                                                              int from, uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr bool kShort = SPAN < L::WIN;
+  __shared__ __align__(8) unsigned long long s_bar;
+  BulkStage sg{&s_bar, 0u, status};
+  if (!DEL) {
+    if (threadIdx.x == 0) mbar_init(&s_bar);
+    __syncthreads();
+  }
   auto one = [&](uint32_t R) {
     // inserts of one round of keys shift the window; deletes, and keys
     // needing several rounds (full window only), re-place every run
     bool ok;
     if constexpr (!DEL) {
-      if (p.region_count[R] <= (uint32_t)L::KMAX) ok = shift_window<LOGS, CNT, SPAN>(loc, p, R);
+      if (p.region_count[R] <= (uint32_t)L::KMAX) ok = shift_window<LOGS, CNT, SPAN>(loc, p, R, sg);
       else ok = kShort ? false : rebuild_window<LOGS, DEL, CNT, SPAN>(loc, p, R);
     } else {
       ok = (kShort && p.region_count[R] > (uint32_t)L::KMAX) ? false
