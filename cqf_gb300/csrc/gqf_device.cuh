@@ -75,15 +75,18 @@ namespace gqf {
 GQF_HD uint64_t bitmask(int n) { return n >= 64 ? ~0ULL : ((1ULL << n) - 1ULL); }
 
 // hash_64 (src/hashutil.cu:132-142): Thomas Wang's invertible 64-bit mix,
-// restricted to the low key_bits bits.
+// restricted to the low key_bits bits.  Its shift-and-add steps are products
+// by constants modulo 2^64, written as such: ~k + (k << 21) = k * (2^21 - 1)
+// - 1, k + (k << 3) + (k << 8) = k * 265, k + (k << 2) + (k << 4) = k * 21,
+// k + (k << 31) = k * (2^31 + 1).
 GQF_HD uint64_t hash64(uint64_t key, uint64_t mask) {
-  key = (~key + (key << 21)) & mask;
+  key = (key * ((1ULL << 21) - 1ULL) - 1ULL) & mask;
   key = key ^ key >> 24;
-  key = ((key + (key << 3)) + (key << 8)) & mask;
+  key = (key * 265ULL) & mask;
   key = key ^ key >> 14;
-  key = ((key + (key << 2)) + (key << 4)) & mask;
+  key = (key * 21ULL) & mask;
   key = key ^ key >> 28;
-  key = (key + (key << 31)) & mask;
+  key = (key * ((1ULL << 31) + 1ULL)) & mask;
   return key;
 }
 
