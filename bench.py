@@ -497,65 +497,73 @@ def run_gpu(args, wl, rank, world):
 
 
 def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
-    """The same step through the C ABI from pinned host buffers: every batch
-    is copied host->device inside the timed region, get results come back
-    device->host.  Inputs go up on one stream and results come down on
-    another, both overlapping the bulk calls on a third."""
+    """The same step through the C ABI from pinned host buffers: every input
+    is copied host->device and every get result device->host inside the timed
+    region, each step.  Insert batches go up through two rotating device
+    buffers on one stream; the get and delete inputs go up on a second stream
+    into buffers of their own while the inserts run (the step's inputs are
+    known when it starts, and the inserts leave the copy engines mostly idle);
+    get results come down on a third stream, chunk by chunk, as the gets
+    finish; the bulk calls run on a fourth."""
     hk = torch.empty(wl.n_insert, dtype=torch.int64, pin_memory=True)
     ha = torch.empty(wl.n_get, dtype=torch.int64, pin_memory=True)
     hk.copy_(keys_dev.cpu())
     ha.copy_(absent_dev.cpu())
     hres = torch.empty(2 * wl.n_get, dtype=torch.int64, pin_memory=True)
-    comp = torch.cuda.Stream()
-    copy = torch.cuda.Stream()
-    down = torch.cuda.Stream()
+    comp, copy, pre, down = (torch.cuda.Stream() for _ in range(4))
     B = wl.batch
     bufs = [torch.empty(B, dtype=torch.int64, device="cuda") for _ in range(2)]
-    outs = [torch.empty(B, dtype=torch.int64, device="cuda") for _ in range(2)]
+    getbuf = torch.empty(2 * wl.n_get, dtype=torch.int64, device="cuda")
+    delbuf = torch.empty(wl.n_get, dtype=torch.int64, device="cuda")
+    resbuf = torch.empty(2 * wl.n_get, dtype=torch.int64, device="cuda")
     copied = [torch.cuda.Event() for _ in range(2)]
     done = [torch.cuda.Event() for _ in range(2)]  # bufs[b] consumed
-    counted = [torch.cuda.Event() for _ in range(2)]  # outs[b] written
-    drained = [torch.cuda.Event() for _ in range(2)]  # outs[b] copied down
-    for e in done:
+    gets_in, dels_in = torch.cuda.Event(), torch.cuda.Event()
+    gets_done, dels_done, drained = torch.cuda.Event(), torch.cuda.Event(), torch.cuda.Event()
+    for e in done + [gets_done, dels_done]:
         e.record(comp)
-    for e in drained:
-        e.record(down)
+    drained.record(down)
     qf.set_stream(comp)
-
-    def phase(chunks, op):
-        for i, (src, s, n) in enumerate(chunks):
-            b = i & 1
-            copy.wait_event(done[b])
-            with torch.cuda.stream(copy):
-                bufs[b][:n].copy_(src[s:s + n], non_blocking=True)
-                copied[b].record(copy)
-            comp.wait_event(copied[b])
-            if op == "insert":
-                qf.bulk_insert_async(bufs[b], n, stream=comp)
-            elif op == "delete":
-                qf.bulk_delete_async(bufs[b], n, stream=comp)
-            else:
-                comp.wait_event(drained[b])
-                qf.bulk_get_async(bufs[b], outs[b], n, stream=comp)
-                counted[b].record(comp)
-                down.wait_event(counted[b])
-                with torch.cuda.stream(down):
-                    off = s + (wl.n_get if src is ha else 0)
-                    hres[off:off + n].copy_(outs[b][:n], non_blocking=True)
-                    drained[b].record(down)
-            done[b].record(comp)
-
-    ins = [(hk, s, n) for s, n in wl.batches]
-    gets = [(hk, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)] + \
-           [(ha, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)]
-    dels = [(hk, s, min(B, wl.n_get - s)) for s in range(0, wl.n_get, B)]
+    get_chunks = [(s, min(B, 2 * wl.n_get - s)) for s in range(0, 2 * wl.n_get, B)]
 
     def step():
         with torch.cuda.stream(comp):
             qf.reset()
-        phase(ins, "insert")
-        phase(gets, "get")
-        phase(dels, "delete")
+        # the get and delete inputs, once the previous step's calls are done with their buffers
+        pre.wait_event(gets_done)
+        with torch.cuda.stream(pre):
+            getbuf[: wl.n_get].copy_(hk[: wl.n_get], non_blocking=True)
+            getbuf[wl.n_get:].copy_(ha, non_blocking=True)
+            gets_in.record(pre)
+        pre.wait_event(dels_done)
+        with torch.cuda.stream(pre):
+            delbuf.copy_(hk[: wl.n_get], non_blocking=True)
+            dels_in.record(pre)
+        for i, (s, n) in enumerate(wl.batches):  # inserts through the rotating buffers
+            b = i & 1
+            copy.wait_event(done[b])
+            with torch.cuda.stream(copy):
+                bufs[b][:n].copy_(hk[s:s + n], non_blocking=True)
+                copied[b].record(copy)
+            comp.wait_event(copied[b])
+            qf.bulk_insert_async(bufs[b], n, stream=comp)
+            done[b].record(comp)
+        comp.wait_event(gets_in)
+        comp.wait_event(drained)  # the previous step's results are down
+        for s, n in get_chunks:
+            qf.bulk_get_async(getbuf[s:s + n], resbuf[s:s + n], n, stream=comp)
+            ev = torch.cuda.Event()
+            ev.record(comp)
+            down.wait_event(ev)
+            with torch.cuda.stream(down):
+                hres[s:s + n].copy_(resbuf[s:s + n], non_blocking=True)
+        drained.record(down)
+        gets_done.record(comp)
+        comp.wait_event(dels_in)
+        for s in range(0, wl.n_get, B):
+            n = min(B, wl.n_get - s)
+            qf.bulk_delete_async(delbuf[s:s + n], n, stream=comp)
+        dels_done.record(comp)
 
     # the first passes over fresh pinned buffers run slower: warm up at
     # least three full steps
@@ -576,7 +584,9 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
         "ms_per_step": round(dt * 1e3, 3),
         "h2d_bytes_per_step": h2d,
         "d2h_bytes_per_step": 8 * 2 * wl.n_get,
-        "path": "C ABI (gqf_bulk_*_async) from pinned host buffers, copies up and down on their own streams",
+        "path": "C ABI (gqf_bulk_*_async) from pinned host buffers: insert batches up through two rotating "
+                "device buffers, the get and delete inputs up on a second stream during the inserts, get "
+                "results down on a third stream as each chunk finishes, bulk calls on a fourth",
         "present_all_found": found,
     }
 
