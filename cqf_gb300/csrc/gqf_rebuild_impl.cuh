@@ -30,6 +30,7 @@
 // cluster length and reports a full table like the reference does.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "gqf_kernels.cuh"
 
@@ -942,17 +943,27 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   // of slot x is max(a, D + b).
   const int ca = tid * qpt;
   const int lo = max(ca, c0 + 1), hi = min(ca + qpt, win_valid);
-  struct Walk {  // per-slot flags, advanced slot by slot from the rank tables
-    int w, o, k;
-    unsigned long long m, ow, tw;
+  // The thread's occupied, runend (after c0) and touched-run bits, from lo
+  // on, in one register each, shifted by one slot per step.
+  using Bits = typename std::conditional<(qpt <= 32), uint32_t, unsigned long long>::type;
+  struct Walk {
+    int o, k;
+    Bits ob, mb, tb;
     bool prev_end, prev_tr;
   };
+  // bits [from, from + n) of a bitmap given word by word (n <= 64, within the window)
+  auto window_bits = [&](auto word, int from, int n) -> Bits {
+    const int w = from >> 6, sh = from & 63;
+    unsigned long long v = word(w) >> sh;
+    if (sh && sh + n > 64) v |= word(w + 1) << (64 - sh);
+    return (Bits)(n >= 64 ? v : v & ((1ULL << n) - 1ULL));
+  };
   auto walk_init = [&](Walk& W) {
-    W.w = lo >> 6;
-    W.m = runs_after_c0(W.w);
-    W.ow = W.w < wq_words ? C.occ(W.w) : 0ULL;
-    W.tw = trm[W.w];
-    W.k = (int)rrank[W.w] + __popcll(W.m & ((1ULL << (lo & 63)) - 1ULL));
+    const int n = hi - lo;
+    W.ob = window_bits([&](int w) { return w < wq_words ? C.occ(w) : 0ULL; }, lo, n);
+    W.mb = window_bits([&](int w) { return runs_after_c0(w); }, lo, n);
+    W.tb = window_bits([&](int w) { return trm[w]; }, lo, n);
+    W.k = (int)rrank[lo >> 6] + __popcll(runs_after_c0(lo >> 6) & ((1ULL << (lo & 63)) - 1ULL));
     W.o = lo < win_q ? rank_of(lo) : nold;  // occupied window quotients below lo
     if (lo == c0 + 1) {
       W.prev_end = false;
@@ -968,16 +979,12 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   // map max(0, D + b)), and whether a touched run's writer needs the shift
   // before it.
   auto step = [&](Walk& W, int x, int& b, bool& used, bool& is_end, bool& tr, bool& evt) {
-    if ((x >> 6) != W.w) {
-      W.w = x >> 6;
-      W.m = runs_after_c0(W.w);
-      W.ow = W.w < wq_words ? C.occ(W.w) : 0ULL;
-      W.tw = trm[W.w];
-    }
-    const int bit = x & 63;
-    W.o += (int)((W.ow >> bit) & 1ULL);
-    is_end = (W.m >> bit) & 1ULL;
-    tr = (W.tw >> bit) & 1ULL;
+    W.o += (int)(W.ob & 1u);
+    is_end = W.mb & 1u;
+    tr = W.tb & 1u;
+    W.ob >>= 1;
+    W.mb >>= 1;
+    W.tb >>= 1;
     const int gv = (int)ins[x];
     evt = gv != 0 || (W.prev_tr && W.prev_end);
     used = W.o > W.k;
