@@ -395,6 +395,15 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
     if (c0 >= lo) rw &= ~0ULL << (c0 - lo + 1);
     return rw;
   };
+  // A thread's bits of a bitmap, [from, from + n) (0 < n <= 64, inside the
+  // window), in one register shifted by one per step of its loops.
+  using Bits = typename std::conditional<(qpt <= 32), uint32_t, unsigned long long>::type;
+  auto window_bits = [&](auto word, int from, int n) -> Bits {
+    const int w = from >> 6, sh = from & 63;
+    unsigned long long v = word(w) >> sh;
+    if (sh && sh + n > 64) v |= word(w + 1) << (64 - sh);
+    return (Bits)(n >= 64 ? v : v & ((1ULL << n) - 1ULL));
+  };
 
   for (uint32_t kr = kbeg; kr < kend && !deferred; kr += KMAX) {
     const int nk = (int)min((uint32_t)KMAX, kend - kr);
@@ -537,16 +546,17 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
       // over its own runs [k0, k1): the run ends other threads read (k0 - 1
       // above, e_old) are read before any is overwritten.
       __syncthreads();
-      unsigned long long ow = 0, tw = 0;
-      int cw = -1;
+      Bits ob = 0, tb = 0;  // occupied and touched quotients from ca on
+      if (ca < qb_) {
+        ob = window_bits([&](int w) { return C.occ(w); }, ca, qb_ - ca);
+        tb = window_bits([&](int w) { return tch[w]; }, ca, qb_ - ca);
+      }
       for (int q = ca; q < qb_; q++) {
-        if ((q >> 6) != cw) {
-          cw = q >> 6;
-          ow = C.occ(cw);
-          tw = q < nq ? tch[cw] : 0ULL;
-        }
+        const bool oq = ob & 1u, tq = tb & 1u;
+        ob >>= 1;
+        tb >>= 1;
         int len = 0;
-        if ((ow >> (q & 63)) & 1ULL) {
+        if (oq) {
           const int e = runpos(k);
           const int s = max(q, pe + 1);
           len = e - s + 1;
@@ -554,7 +564,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
           pe = e;
           k++;
         }
-        if ((tw >> (q & 63)) & 1ULL) len = pref[q];
+        if (tq) len = pref[q];
         pref[q] = (uint16_t)len;
         if (len > 0) { fa = max(q + len - 1, fa + len); fb += len; }
       }
@@ -578,20 +588,26 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
     {
       int x = max(fa, c0 + fb);  // end of all runs before this thread's first quotient
       int k = k0;
-      unsigned long long occ_bits = 0, ow = 0, tw = 0;
+      unsigned long long occ_bits = 0;
       int occ_word = ca >> 6, cw = -1;
       unsigned long long ebits = 0;  // new runend bits of window word ew
       int ew = -1;
       int nlen = ca < qb_ ? pref[ca] : 0;  // the next quotient's length, loaded a step ahead
       int nd = delta[k];                   // the next run's old start, loaded ahead
+      Bits ob = 0, tb = 0;  // occupied and touched quotients from ca on
+      if (ca < qb_) {
+        ob = window_bits([&](int w) { return C.occ(w); }, ca, qb_ - ca);
+        tb = window_bits([&](int w) { return tch[w]; }, ca, qb_ - ca);
+      }
       for (int q = ca; q < qb_; q++) {
         if ((q >> 6) != cw) {
           if (cw >= 0 && occ_bits) or64(&nocc[occ_word], occ_bits);
           occ_bits = 0;
           cw = occ_word = q >> 6;
-          ow = C.occ(cw);
-          tw = q < nq ? tch[cw] : 0ULL;
         }
+        const bool oq = ob & 1u, tq = tb & 1u;
+        ob >>= 1;
+        tb >>= 1;
         const int len = nlen;
         if (q + 1 < qb_) nlen = pref[q + 1];
         const int ns = max(q, x + 1);
@@ -607,8 +623,8 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
             ebits |= 1ULL << (x & 63);
           }
         }
-        if ((ow >> (q & 63)) & 1ULL) {
-          delta[k] = (int16_t)(((tw >> (q & 63)) & 1ULL) ? kTouched + nd : ns - nd);
+        if (oq) {
+          delta[k] = (int16_t)(tq ? kTouched + nd : ns - nd);
           k++;
           nd = delta[k];
         }
@@ -649,18 +665,14 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
     {
       const int cb = min(ca + qpt, wslots);
       if (ca < cb) {
-        int w = ca >> 6;
-        unsigned long long m = runs_after_c0(C, w);
-        unsigned long long ow = w < wq_words ? C.occ(w) : 0ULL;
-        int k = rrank[w] + __popcll(m & ((1ULL << (ca & 63)) - 1ULL));
+        const int w = ca >> 6;
+        int k = rrank[w] + __popcll(runs_after_c0(C, w) & ((1ULL << (ca & 63)) - 1ULL));
         int o = ca < win_q ? rank_of(ca) : nold;  // occupied window quotients below sl
+        Bits mb = window_bits([&](int ww) { return runs_after_c0(C, ww); }, ca, cb - ca);
+        Bits ob = window_bits([&](int ww) { return ww < wq_words ? C.occ(ww) : 0ULL; }, ca, cb - ca);
         for (int sl = ca; sl < cb; sl++) {
-          if ((sl >> 6) != w) {
-            w = sl >> 6;
-            m = runs_after_c0(C, w);
-            ow = w < wq_words ? C.occ(w) : 0ULL;
-          }
-          o += (int)((ow >> (sl & 63)) & 1ULL);
+          o += (int)(ob & 1u);
+          ob >>= 1;
           if (sl > c0 && o > k) {
             const int d = delta[k];
             if (d < kTouched) {
@@ -668,7 +680,8 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
               if (t >= 0 && t < wslots) N.slot(t) = C.slot(sl);
             }
           }
-          k += (int)((m >> (sl & 63)) & 1ULL);
+          k += (int)(mb & 1u);
+          mb >>= 1;
         }
       }
     }
