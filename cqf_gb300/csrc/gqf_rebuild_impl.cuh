@@ -155,14 +155,31 @@ constexpr int kListCount = 0, kListNext = 1, kListBase = 2;
 
 // ----------------------------------------------------- shared-memory image
 
+// A window in shared memory in split form: the slots contiguous (slot i of
+// the window at s[i]) and the blocks' 32-byte headers after them (header w
+// at h + 32 w: occupieds, runends, offset), so that the per-slot loops index
+// one byte instead of recomputing a block address.  The image of WB blocks
+// takes the same 96 WB bytes as the blocks themselves.
 struct Img {
-  uint8_t* p;
-  __device__ uint8_t& slot(int i) const { return p[(i >> 6) * 96 + 32 + (i & 63)]; }
-  __device__ unsigned long long& occ(int w) const { return *reinterpret_cast<unsigned long long*>(p + w * 96); }
-  __device__ unsigned long long& run(int w) const { return *reinterpret_cast<unsigned long long*>(p + w * 96 + 8); }
-  __device__ uint32_t& off(int w) const { return *reinterpret_cast<uint32_t*>(p + w * 96 + 16); }
+  uint8_t* s;
+  uint8_t* h;
+  __device__ uint8_t& slot(int i) const { return s[i]; }
+  __device__ unsigned long long& occ(int w) const { return *reinterpret_cast<unsigned long long*>(h + w * 32); }
+  __device__ unsigned long long& run(int w) const { return *reinterpret_cast<unsigned long long*>(h + w * 32 + 8); }
+  __device__ uint32_t& off(int w) const { return *reinterpret_cast<uint32_t*>(h + w * 32 + 16); }
   __device__ int is_end(int i) const { return (int)((run(i >> 6) >> (i & 63)) & 1ULL); }
+  // The place in this image of 16-byte word i of the same window laid out
+  // as blocks (word 6 w + c of block w: c = 0, 1 its header, 2-5 its slots).
+  __device__ uint4& part(int i) const {
+    const int w = i / 6, c = i - 6 * w;
+    return c < 2 ? reinterpret_cast<uint4*>(h + w * 32)[c] : reinterpret_cast<uint4*>(s + w * 64)[c - 2];
+  }
 };
+// The image of a window of WB blocks at `base` (16-byte aligned).
+template <int WB>
+__device__ __forceinline__ Img img_at(uint8_t* base) {
+  return Img{base, base + WB * 64};
+}
 
 // Merge one run's old counters with the run's new keys (sorted by remainder;
 // each key counts once, or cnts[j] times when cnts is given) and return the
@@ -374,11 +391,11 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
   // ---- stage the window (wb blocks of 96 bytes) into image 0
   {
     const uint4* src = reinterpret_cast<const uint4*>(g.blocks + bw0);
-    uint4* dst = reinterpret_cast<uint4*>(sm + L::OFF_IMG0);
-    for (int i = tid; i < wb * 6; i += NT) dst[i] = src[i];
+    const Img D = img_at<WB>(sm + L::OFF_IMG0);
+    for (int i = tid; i < wb * 6; i += NT) D.part(i) = src[i];
   }
   __syncthreads();
-  const int c0 = (int)Img{sm + L::OFF_IMG0}.off(0) - 1;  // last slot used by earlier regions' runs
+  const int c0 = (int)img_at<WB>(sm + L::OFF_IMG0).off(0) - 1;  // last slot used by earlier regions' runs
   // The previous region's runs fill the whole window: every run of this
   // region lies beyond it, so only the serial path can place them.  (This
   // also keeps all window positions far below the 16-bit tables' range.)
@@ -407,8 +424,8 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
 
   for (uint32_t kr = kbeg; kr < kend && !deferred; kr += KMAX) {
     const int nk = (int)min((uint32_t)KMAX, kend - kr);
-    const Img C{sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0)};
-    const Img N{sm + (cur ? L::OFF_IMG0 : L::OFF_IMG1)};
+    const Img C = img_at<WB>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
+    const Img N = img_at<WB>(sm + (cur ? L::OFF_IMG0 : L::OFF_IMG1));
 
     // ---- group this round's keys by quotient (counting sort in shared memory)
     for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
@@ -573,10 +590,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
     // ---- run positions: one block-wide max-plus scan over the quotients
     scan_maps<NT>(fa, fb, sa, sb);
     // ---- clear the next image; keep the previous region's spill
-    {
-      uint4* dst = reinterpret_cast<uint4*>(N.p);
-      for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
-    }
+    for (int i = tid; i < wb * 6; i += NT) N.part(i) = make_uint4(0, 0, 0, 0);
     __syncthreads();
     for (int sl = tid; sl <= c0 && sl < wslots; sl += NT) N.slot(sl) = C.slot(sl);
     for (int w = tid; w < wb && 64 * w <= c0; w += NT) {
@@ -706,18 +720,18 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
   if (!changed) return true;
   // ---- write back the blocks that differ from what was loaded
   {
-    const uint4* fin = reinterpret_cast<const uint4*>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
-    const uint4* org = reinterpret_cast<const uint4*>(sm + L::OFF_IMG0);
+    const Img fin = img_at<WB>(sm + (cur ? L::OFF_IMG1 : L::OFF_IMG0));
+    const Img org = img_at<WB>(sm + L::OFF_IMG0);
     uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0);
     for (int w = tid; w < wb; w += NT) {
       bool diff = multi;  // after several rounds the loaded image is gone
       if (!diff)
         for (int c = 0; c < 6; c++) {
-          uint4 a = fin[w * 6 + c], b = org[w * 6 + c];
+          const uint4 a = fin.part(w * 6 + c), b = org.part(w * 6 + c);
           diff |= (a.x != b.x) | (a.y != b.y) | (a.z != b.z) | (a.w != b.w);
         }
       if (diff)
-        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
+        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin.part(w * 6 + c);
     }
   }
   return true;
@@ -786,8 +800,8 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   const int win_q = (int)min((uint64_t)SPAN, g.nslots - base);
   const int wq_words = (win_q + 63) >> 6;
 
-  const Img C{sm + L::OFF_IMG0};
-  const Img N{sm + L::OFF_IMG1};
+  const Img C = img_at<WB>(sm + L::OFF_IMG0);
+  const Img N = img_at<WB>(sm + L::OFF_IMG1);
   uint32_t* kg = reinterpret_cast<uint32_t*>(sm + L::OFF_KG);
   uint32_t* kc = reinterpret_cast<uint32_t*>(sm + L::OFF_KC);
   // growth entering before each slot, then the shift just before it
@@ -803,14 +817,18 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   uint16_t* rrank = reinterpret_cast<uint16_t*>(sm + L::OFF_RRANK);
   uint32_t* kn = CNT ? reinterpret_cast<uint32_t*>(sm + L::OFF_KN) : nullptr;
 
-  // ---- stage the window (wb blocks of 96 bytes) into image C with one
-  // bulk copy, clearing the tables meanwhile
-  if (tid == 0) bulk_stage_start(sg, C.p, g.blocks + bw0, (uint32_t)wb * 96u);
+  // ---- stage the window (wb blocks of 96 bytes) with one bulk copy into
+  // image N's memory, clearing the tables meanwhile, then split it into
+  // image C (N is cleared before its first use)
+  const uint4* raw = reinterpret_cast<const uint4*>(sm + L::OFF_IMG1);
+  if (tid == 0) bulk_stage_start(sg, sm + L::OFF_IMG1, g.blocks + bw0, (uint32_t)wb * 96u);
   for (int i = tid; i < L::KCW; i += NT) kc[i] = 0;
   for (int i = tid; i < (wslots >> 1); i += NT) ins32[i] = 0;
   const bool staged = bulk_stage_wait(sg);
   __syncthreads();
   if (!staged) return false;
+  for (int i = tid; i < wb * 6; i += NT) C.part(i) = raw[i];
+  __syncthreads();
   const int c0 = (int)C.off(0) - 1;  // last slot used by earlier regions' runs
   if (c0 + 1 >= win_valid) return false;  // every run of this region lies past the window
 
@@ -1023,10 +1041,7 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   const int d_in = max(ea, eb);  // the shift entering this thread's slots (D = 0 before the window)
   if (tid == NT - 1) s_i[2] = max(fa, sat(d_in + fb));  // the shift after the window's last slot
   // ---- clear the new image; keep the previous region's spill
-  {
-    uint4* dst = reinterpret_cast<uint4*>(N.p);
-    for (int i = tid; i < wb * 6; i += NT) dst[i] = make_uint4(0, 0, 0, 0);
-  }
+  for (int i = tid; i < wb * 6; i += NT) N.part(i) = make_uint4(0, 0, 0, 0);
   __syncthreads();
   if (s_i[2] != 0) return false;  // the changes reach past the window
   for (int sl = tid; sl <= c0 && sl < wslots; sl += NT) N.slot(sl) = C.slot(sl);
@@ -1142,17 +1157,15 @@ __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p,
   __syncthreads();
   // ---- write back the blocks that differ from what was loaded
   {
-    const uint4* fin = reinterpret_cast<const uint4*>(N.p);
-    const uint4* org = reinterpret_cast<const uint4*>(C.p);
     uint4* dst = reinterpret_cast<uint4*>(g.blocks + bw0);
     for (int w = tid; w < wb; w += NT) {
       bool diff = false;
       for (int c = 0; c < 6; c++) {
-        const uint4 a = fin[w * 6 + c], b = org[w * 6 + c];
+        const uint4 a = N.part(w * 6 + c), b = C.part(w * 6 + c);
         diff |= (a.x != b.x) | (a.y != b.y) | (a.z != b.z) | (a.w != b.w);
       }
       if (diff)
-        for (int c = 0; c < 6; c++) dst[w * 6 + c] = fin[w * 6 + c];
+        for (int c = 0; c < 6; c++) dst[w * 6 + c] = N.part(w * 6 + c);
     }
   }
   return true;
