@@ -99,15 +99,22 @@ __device__ __forceinline__ bool bulk_stage_wait(BulkStage& sg) {
 template <int LOGS>
 struct Cfg;
 // PUSH: the slots past the region a window holds; TAIL: the shorter tail
-// tried first, enough whenever the region's growth is absorbed that close.
+// tried first, enough whenever the region's growth is absorbed that close;
+// MINB: CTAs per SM the kernels are built for; MINB_INS: the short-window
+// insert kernel's (its shared memory allows five at 2^12 quotients, where
+// 48 registers cost it 8 bytes of spills; the delete kernel spills 64 bytes
+// there and runs faster at four).
 template <>
-struct Cfg<11> { static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4; };
+struct Cfg<11> { static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 4; };
 template <>
-struct Cfg<12> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 2048, MINB = 4; };
+struct Cfg<12> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 5; };
 template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 4096, MINB = 2; };
+struct Cfg<13> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 4096, MINB = 2, MINB_INS = 2; };
 
-template <int LOGS, bool CNT>
+// The layout of one kernel's shared memory.  Its tables are sized for the
+// window span TS the kernel works in (the short or the full window), so the
+// short-window kernels take less shared memory and more of them fit an SM.
+template <int LOGS, bool CNT, int TS = (1 << LOGS) + Cfg<LOGS>::PUSH>
 struct Lay {
   static constexpr int NT = 256;
   static constexpr int REG = 1 << LOGS;
@@ -115,11 +122,12 @@ struct Lay {
   static constexpr int KMAX = Cfg<LOGS>::KMAX;
   static constexpr int WIN = REG + PUSH;
   static constexpr int SHORT = REG + Cfg<LOGS>::TAIL;
-  static constexpr int WB = WIN / 64;
+  static constexpr int WB = TS / 64;
   static constexpr int KCW = REG / 2 + 2;  // packed 16-bit per-quotient key counters
   static_assert(WIN % NT == 0 && SHORT % NT == 0 && SHORT <= WIN && (REG / 2) % NT == 0,
                 "work splits evenly over threads");
-  static_assert(KCW * 4 <= (WIN + 8) * 2, "the key counters fit the shift table they share");
+  static_assert(TS % NT == 0 && TS >= SHORT && TS <= WIN, "a table span is the short or the full window");
+  static_assert(KCW * 4 <= (TS + 8) * 2, "the key counters fit the shift table they share");
   static_assert(PUSH < REG, "a window must not reach the region after next");
   static_assert(WIN + PUSH + 64 < 32767, "window positions fit int16");
   static_assert(WB < NT, "window words fit one scan");
@@ -129,14 +137,14 @@ struct Lay {
   static constexpr int OFF_IMG0 = 0;
   static constexpr int OFF_IMG1 = OFF_IMG0 + IMG;
   static constexpr int OFF_KG = OFF_IMG1 + IMG;                  // u32[KMAX] keys grouped by quotient
-  static constexpr int OFF_PREF = OFF_KG + KMAX * 4;             // u16[WIN] lengths, then ends + 1
+  static constexpr int OFF_PREF = OFF_KG + KMAX * 4;             // u16[TS] lengths, then ends + 1
   // one table, three lives: the key counters while the keys are grouped,
   // then the old run ends by rank, then each old run's start and shift
-  static constexpr int OFF_DELTA = OFF_PREF + WIN * 2;           // i16[WIN + 8]
+  static constexpr int OFF_DELTA = OFF_PREF + TS * 2;            // i16[TS + 8]
   static constexpr int OFF_KC = OFF_DELTA;                       // u32[KCW]
-  static constexpr int OFF_RPOS = OFF_DELTA;                     // u16[WIN + 8]
+  static constexpr int OFF_RPOS = OFF_DELTA;                     // u16[TS + 8]
   // the single-round kernel keeps two u16 per key in the same table
-  static constexpr int DELTA_BYTES = (WIN + 8) * 2 > 4 * KMAX ? (WIN + 8) * 2 : 4 * KMAX;
+  static constexpr int DELTA_BYTES = (TS + 8) * 2 > 4 * KMAX ? (TS + 8) * 2 : 4 * KMAX;
   static constexpr int OFF_NOCC = (OFF_DELTA + DELTA_BYTES + 7) & ~7;  // u64[WB] new occupieds
   static constexpr int OFF_TCH = OFF_NOCC + WB * 8;              // u64[WB] touched quotients
   static constexpr int OFF_ORANK = OFF_TCH + WB * 8;             // u16[WB + 8]
@@ -353,7 +361,7 @@ __device__ int scan_sum(int v, int* tmp, int* total) {
 // the window.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
 __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& p, const uint32_t R) {
-  using L = Lay<LOGS, CNT>;
+  using L = Lay<LOGS, CNT, SPAN>;
   constexpr int NT = L::NT, WB = L::WB, REG = L::REG, KMAX = L::KMAX, span = SPAN;
   constexpr int qpt = SPAN / NT;  // slots and quotients per thread
   extern __shared__ __align__(128) uint8_t sm[];
@@ -773,7 +781,7 @@ __device__ __forceinline__ int rank_word(const uint16_t* rank, int nw, int k) {
 // KMAX keys, go to rebuild_window.
 template <int LOGS, bool CNT, int SPAN, class Loc>
 __device__ __forceinline__ bool shift_window(const Loc& loc, const Partition& p, const uint32_t R, BulkStage& sg) {
-  using L = Lay<LOGS, CNT>;
+  using L = Lay<LOGS, CNT, SPAN>;
   constexpr int NT = L::NT, WB = L::WB, REG = L::REG, KMAX = L::KMAX;
   constexpr int qpt = SPAN / NT;  // slots per thread
   constexpr int kFar = 1 << 20;   // a position past every window
@@ -1182,8 +1190,10 @@ enum : int { kFromGrid = 0, kFromList = 1, kFromRetry = 2 };
 // hold, and those whose keys need several rounds (they may grow further);
 // the full pass leaves what it cannot hold to the serial fallback.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
-__global__ void __launch_bounds__(256, CNT ? 3 : Cfg<LOGS>::MINB) k_rebuild(Loc loc, Partition p, int parity,
-                                                                             int from, uint32_t* status) {
+__global__ void __launch_bounds__(256, CNT ? 3
+                                          : (!DEL && SPAN < (1 << LOGS) + Cfg<LOGS>::PUSH ? Cfg<LOGS>::MINB_INS
+                                                                                          : Cfg<LOGS>::MINB))
+    k_rebuild(Loc loc, Partition p, int parity, int from, uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr bool kShort = SPAN < L::WIN;
   __shared__ __align__(8) unsigned long long s_bar;
@@ -1339,7 +1349,7 @@ void configure() {
   static std::atomic<bool> done[kMaxDevices];
   once_per_device(done, [] {
     cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         Lay<LOGS, CNT>::BYTES);
+                         Lay<LOGS, CNT, SPAN>::BYTES);
     cudaFuncSetAttribute(k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          100);
   });
@@ -1354,7 +1364,7 @@ uint32_t resident() {
   if (!v) {
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild<LOGS, DEL, CNT, SPAN, Loc>, 256,
-                                                  Lay<LOGS, CNT>::BYTES);
+                                                  Lay<LOGS, CNT, SPAN>::BYTES);
     v = (uint32_t)std::max(1, sm_count()) * (uint32_t)std::max(1, per);
     n[d].store(v, std::memory_order_relaxed);
   }
@@ -1369,12 +1379,13 @@ void launch_passes(const Loc& loc, const Partition& p, int parity, int use_list,
   using L = Lay<LOGS, CNT>;
   configure<LOGS, DEL, CNT, L::SHORT, Loc>();
   configure<LOGS, DEL, CNT, L::WIN, Loc>();
+  constexpr int kShortBytes = Lay<LOGS, CNT, L::SHORT>::BYTES, kFullBytes = Lay<LOGS, CNT, L::WIN>::BYTES;
   const uint32_t g1 = use_list ? std::min(grid, resident<LOGS, DEL, CNT, L::SHORT, Loc>()) : grid;
-  k_rebuild<LOGS, DEL, CNT, L::SHORT, Loc><<<g1, 256, L::BYTES, st>>>(loc, p, parity,
-                                                                      use_list ? kFromList : kFromGrid, status);
+  k_rebuild<LOGS, DEL, CNT, L::SHORT, Loc><<<g1, 256, kShortBytes, st>>>(loc, p, parity,
+                                                                         use_list ? kFromList : kFromGrid, status);
   count_launch();
   const uint32_t g2 = std::min(grid, resident<LOGS, DEL, CNT, L::WIN, Loc>());
-  k_rebuild<LOGS, DEL, CNT, L::WIN, Loc><<<g2, 256, L::BYTES, st>>>(loc, p, parity, kFromRetry, status);
+  k_rebuild<LOGS, DEL, CNT, L::WIN, Loc><<<g2, 256, kFullBytes, st>>>(loc, p, parity, kFromRetry, status);
   count_launch();
 }
 
