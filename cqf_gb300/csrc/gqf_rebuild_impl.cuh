@@ -100,16 +100,28 @@ template <int LOGS>
 struct Cfg;
 // PUSH: the slots past the region a window holds; TAIL: the shorter tail
 // tried first, enough whenever the region's growth is absorbed that close;
-// MINB: CTAs per SM the kernels are built for; MINB_INS: the short-window
-// insert kernel's (its shared memory allows five at 2^12 quotients, where
-// 48 registers cost it 8 bytes of spills; the delete kernel spills 64 bytes
-// there and runs faster at four).
+// MINB: CTAs per SM the kernels are built for; MINB_INS / MINB_CNT: the
+// short-window insert / counted-insert kernels' (their shared memory allows
+// five / four at 2^11 and 2^12 quotients; the delete kernel spills 64 bytes
+// at five and runs faster at four).
 template <>
-struct Cfg<11> { static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 4; };
+struct Cfg<11> {
+  static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 5, MINB_CNT = 4;
+};
 template <>
-struct Cfg<12> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 5; };
+struct Cfg<12> {
+  static constexpr int PUSH = 2048, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 5, MINB_CNT = 4;
+};
 template <>
-struct Cfg<13> { static constexpr int PUSH = 2048, TAIL = 256, KMAX = 4096, MINB = 2, MINB_INS = 2; };
+struct Cfg<13> {
+  static constexpr int PUSH = 2048, TAIL = 256, KMAX = 4096, MINB = 2, MINB_INS = 2, MINB_CNT = 2;
+};
+// CTAs per SM a rebuild kernel is built for.
+template <int LOGS, bool DEL, bool CNT, int SPAN>
+constexpr int rebuild_min_blocks() {
+  constexpr bool kShort = SPAN < (1 << LOGS) + Cfg<LOGS>::PUSH;
+  return CNT ? (kShort ? Cfg<LOGS>::MINB_CNT : 3) : (!DEL && kShort ? Cfg<LOGS>::MINB_INS : Cfg<LOGS>::MINB);
+}
 
 // The layout of one kernel's shared memory.  Its tables are sized for the
 // window span TS the kernel works in (the short or the full window), so the
@@ -1190,9 +1202,7 @@ enum : int { kFromGrid = 0, kFromList = 1, kFromRetry = 2 };
 // hold, and those whose keys need several rounds (they may grow further);
 // the full pass leaves what it cannot hold to the serial fallback.
 template <int LOGS, bool DEL, bool CNT, int SPAN, class Loc>
-__global__ void __launch_bounds__(256, CNT ? 3
-                                          : (!DEL && SPAN < (1 << LOGS) + Cfg<LOGS>::PUSH ? Cfg<LOGS>::MINB_INS
-                                                                                          : Cfg<LOGS>::MINB))
+__global__ void __launch_bounds__(256, (rebuild_min_blocks<LOGS, DEL, CNT, SPAN>()))
     k_rebuild(Loc loc, Partition p, int parity, int from, uint32_t* status) {
   using L = Lay<LOGS, CNT>;
   constexpr bool kShort = SPAN < L::WIN;
