@@ -114,8 +114,8 @@ HostFilter* lookup(const QF* qf) {
 }
 
 int auto_log_region(int nbits) {
-  // 2^12-quotient regions fit four rebuild CTAs per SM and measured fastest
-  // on large tables; small tables use 2^11 for more regions per phase.
+  // 2^12-quotient regions fit four or five rebuild CTAs per SM and measured
+  // fastest on large tables; small tables use 2^11 for more regions per phase.
   return nbits >= 21 ? 12 : 11;
 }
 
