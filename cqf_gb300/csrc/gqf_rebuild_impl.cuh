@@ -100,10 +100,11 @@ template <int LOGS>
 struct Cfg;
 // PUSH: the slots past the region a window holds; TAIL: the shorter tail
 // tried first, enough whenever the region's growth is absorbed that close;
-// MINB: CTAs per SM the kernels are built for; MINB_INS / MINB_CNT: the
-// short-window insert / counted-insert kernels' (their shared memory allows
-// five / four at 2^11 and 2^12 quotients; the delete kernel spills 64 bytes
-// at five and runs faster at four).
+// MINB: CTAs per SM the full-window kernels are built for; MINB_INS /
+// MINB_CNT: the short-window insert and delete / counted-insert kernels'
+// (their shared memory allows five / four at 2^11 and 2^12 quotients; the
+// delete kernel keeps its quotient and slot loops rolled to fit 48
+// registers).
 template <>
 struct Cfg<11> {
   static constexpr int PUSH = 1024, TAIL = 256, KMAX = 2048, MINB = 4, MINB_INS = 5, MINB_CNT = 4;
@@ -120,7 +121,7 @@ struct Cfg<13> {
 template <int LOGS, bool DEL, bool CNT, int SPAN>
 constexpr int rebuild_min_blocks() {
   constexpr bool kShort = SPAN < (1 << LOGS) + Cfg<LOGS>::PUSH;
-  return CNT ? (kShort ? Cfg<LOGS>::MINB_CNT : 3) : (!DEL && kShort ? Cfg<LOGS>::MINB_INS : Cfg<LOGS>::MINB);
+  return CNT ? (kShort ? Cfg<LOGS>::MINB_CNT : 3) : (kShort ? Cfg<LOGS>::MINB_INS : Cfg<LOGS>::MINB);
 }
 
 // The layout of one kernel's shared memory.  Its tables are sized for the
@@ -588,6 +589,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
         ob = window_bits([&](int w) { return C.occ(w); }, ca, qb_ - ca);
         tb = window_bits([&](int w) { return tch[w]; }, ca, qb_ - ca);
       }
+      #pragma unroll 1  // rolled: fewer registers, five CTAs per SM
       for (int q = ca; q < qb_; q++) {
         const bool oq = ob & 1u, tq = tb & 1u;
         ob >>= 1;
@@ -633,6 +635,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
         ob = window_bits([&](int w) { return C.occ(w); }, ca, qb_ - ca);
         tb = window_bits([&](int w) { return tch[w]; }, ca, qb_ - ca);
       }
+      #pragma unroll 1  // rolled: fewer registers, five CTAs per SM
       for (int q = ca; q < qb_; q++) {
         if ((q >> 6) != cw) {
           if (cw >= 0 && occ_bits) or64(&nocc[occ_word], occ_bits);
@@ -704,6 +707,7 @@ __device__ __forceinline__ bool rebuild_window(const Loc& loc, const Partition& 
         int o = ca < win_q ? rank_of(ca) : nold;  // occupied window quotients below sl
         Bits mb = window_bits([&](int ww) { return runs_after_c0(C, ww); }, ca, cb - ca);
         Bits ob = window_bits([&](int ww) { return ww < wq_words ? C.occ(ww) : 0ULL; }, ca, cb - ca);
+        #pragma unroll 1  // rolled: fewer registers, five CTAs per SM
         for (int sl = ca; sl < cb; sl++) {
           o += (int)(ob & 1u);
           ob >>= 1;
