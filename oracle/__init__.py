@@ -5,7 +5,7 @@ reference counting quotient filter, src/gqf.cu) and for ``oracle/_ref`` (the
 reference's own host path compiled from its sources on an x86 host).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg may import this package, and only as the checker or the timed CPU
+leg may import this package, and only as the test oracle or the timed CPU
 baseline.  The product (``cqf_gb300``) never imports it.
 """
 from __future__ import annotations

@@ -4,7 +4,7 @@
  * (PASSIONLab/cqf) on its own packed storage format.  Each function names the
  * reference function it restates (src/gqf.cu unless noted).  Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this code,
- * as the checker or as the timed CPU baseline; the product never calls it.
+ * as the test oracle or as the timed CPU baseline; the product never calls it.
  *
  * Deviations from the reference, none of which change a result the reference
  * produces without crashing:

@@ -5,8 +5,8 @@
  * on the reference's own storage format: packed 81-byte blocks
  * (include/gqf_int.cuh:38-57) behind a 120-byte metadata header
  * (include/gqf_int.cuh:96-113).  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load it, and only as a checker or a timed
- * CPU baseline; the product never calls it.
+ * CPU-baseline leg of bench.py may load it, and only as the test oracle or a
+ * timed CPU baseline; the product never calls it.
  *
  * Pinned against the reference itself: tests/test_oracle.py compares it word
  * for word with oracle/_ref (the reference compiled from its sources here,
