@@ -501,8 +501,9 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
     is copied host->device and every get result device->host inside the timed
     region, each step.  Insert batches go up through two rotating device
     buffers on one stream; the get and delete inputs go up on a second stream
-    into buffers of their own while the inserts run (the step's inputs are
-    known when it starts, and the inserts leave the copy engines mostly idle);
+    into buffers of their own, chunk by chunk between the insert batches (the
+    step's inputs are known when it starts, and the inserts leave the copy
+    engines mostly idle);
     get results come down on a third stream, chunk by chunk, as the gets
     finish; the bulk calls run on a fourth."""
     hk = torch.empty(wl.n_insert, dtype=torch.int64, pin_memory=True)
@@ -526,19 +527,37 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
     qf.set_stream(comp)
     get_chunks = [(s, min(B, 2 * wl.n_get - s)) for s in range(0, 2 * wl.n_get, B)]
 
+    # the get and delete inputs go up in batch-sized chunks, one after each
+    # insert batch's copy, so that the copy engines alternate between the two
+    # and no insert waits behind the whole 1.6 GB (a step that starts on idle
+    # engines would otherwise queue its first inserts behind them)
+    ups = []
+    for s in range(0, wl.n_get, B):
+        ups.append(("get", getbuf[s:s + min(B, wl.n_get - s)], hk[s:s + min(B, wl.n_get - s)]))
+    for s in range(0, wl.n_get, B):
+        n = min(B, wl.n_get - s)
+        ups.append(("get", getbuf[wl.n_get + s:wl.n_get + s + n], ha[s:s + n]))
+    for s in range(0, wl.n_get, B):
+        ups.append(("del", delbuf[s:s + min(B, wl.n_get - s)], hk[s:s + min(B, wl.n_get - s)]))
+    first_del = next(j for j, u in enumerate(ups) if u[0] == "del")
+
+    def upload(j):
+        # each buffer is refilled once the previous step's calls are done with it
+        if j == 0:
+            pre.wait_event(gets_done)
+        if j == first_del:
+            pre.wait_event(dels_done)
+        with torch.cuda.stream(pre):
+            ups[j][1].copy_(ups[j][2], non_blocking=True)
+            if j == first_del - 1:
+                gets_in.record(pre)
+            if j == len(ups) - 1:
+                dels_in.record(pre)
+
     def step():
         with torch.cuda.stream(comp):
             qf.reset()
-        # the get and delete inputs, once the previous step's calls are done with their buffers
-        pre.wait_event(gets_done)
-        with torch.cuda.stream(pre):
-            getbuf[: wl.n_get].copy_(hk[: wl.n_get], non_blocking=True)
-            getbuf[wl.n_get:].copy_(ha, non_blocking=True)
-            gets_in.record(pre)
-        pre.wait_event(dels_done)
-        with torch.cuda.stream(pre):
-            delbuf.copy_(hk[: wl.n_get], non_blocking=True)
-            dels_in.record(pre)
+        j = 0
         for i, (s, n) in enumerate(wl.batches):  # inserts through the rotating buffers
             b = i & 1
             copy.wait_event(done[b])
@@ -548,6 +567,12 @@ def run_e2e(args, wl, qf, keys_dev, absent_dev, torch, dist=None, world=1):
             comp.wait_event(copied[b])
             qf.bulk_insert_async(bufs[b], n, stream=comp)
             done[b].record(comp)
+            if i >= 1 and j < len(ups):
+                upload(j)
+                j += 1
+        while j < len(ups):
+            upload(j)
+            j += 1
         comp.wait_event(gets_in)
         comp.wait_event(drained)  # the previous step's results are down
         for s, n in get_chunks:
